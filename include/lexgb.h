@@ -1,0 +1,150 @@
+/*
+ * lexgb.h - C ABI of lex_gb300, a GB300 (sm_103a) implementation of LEX's fully
+ * compressible dynamical-core time step (solver_opt = 2: explicit time splitting,
+ * WENO5 advection, Smagorinsky SGS, acoustic sub-steps, pressure gradient, Coriolis,
+ * periodic / rigid-lid halos, Wicker-Skamarock RK3).
+ *
+ * Conventions
+ *   - Every call returns int status: LEXGB_OK (0) or an LEXGB_ERR_* code; the message of
+ *     the last failure on the calling thread is available from lexgb_last_error().
+ *   - Host arrays use the reference's padded C-order [x][y][z] layout (z fastest) with
+ *     ngx = ngy = 3 lateral ghost cells and ngz = 1 ghost level:
+ *        scalars (theta, pi', qv)  (nx+6) x (ny+6) x (nz+2)
+ *        u                         (nx+7) x (ny+6) x (nz+2)
+ *        v                         (nx+6) x (ny+7) x (nz+2)
+ *        w                         (nx+6) x (ny+6) x (nz+3)
+ *     exactly as setup_lex.py:39-49 allocates them.  Ghost values on input are ignored
+ *     (they are periodic / edge copies by construction); on output they are filled the way
+ *     padding3_array / padding3u_array / padding3v_array + set_w_bc fill them.
+ *   - Field order is the reference's phys_state tuple: (theta, u, v, w, pi', qv)
+ *     (setup_lex.py:66).
+ *   - Device memory is owned by the context.  A context is not thread-safe; all its work
+ *     is ordered on one CUDA stream (its own, or the one given to lexgb_set_stream).
+ */
+#ifndef LEXGB_H
+#define LEXGB_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    LEXGB_OK = 0,
+    LEXGB_ERR_ARG = 1,      /* bad dimensions, null pointer, out-of-range option */
+    LEXGB_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+    LEXGB_ERR_NAN = 3,      /* a non-finite value was found in the state */
+    LEXGB_ERR_TIMEOUT = 4,  /* a bounded device-side wait gave up */
+    LEXGB_ERR_STATE = 5,    /* call order violated (e.g. stepping before a base state is set) */
+    LEXGB_ERR_ALLOC = 6     /* device allocation failed */
+};
+
+enum { LEXGB_F32 = 0, LEXGB_F64 = 1 };
+
+typedef struct lexgb_config {
+    int nx, ny, nz;          /* interior cells; nx, ny >= 4, nz >= 6 */
+    double dx, dy, dz;       /* uniform spacings [m] (namelist_n_constants.py:17-19) */
+    double dt;               /* RK3 big-step length [s] (namelist_n_constants.py:7) */
+    int n_sound;             /* acoustic sub-steps per big step (namelist_n_constants.py:13) */
+    int turb_opt;            /* 0: none, 1: Smagorinsky (namelist_n_constants.py:48) */
+    int cor_opt;             /* 0: none, 1: Coriolis, 2: Coriolis + large-scale pressure gradient */
+    double f_cor;            /* Coriolis parameter (namelist_n_constants.py:39) */
+    double theta_ref;        /* constant subtracted from theta on the device; 0 = use theta0 at the first level */
+} lexgb_config;
+
+typedef struct lexgb_ctx lexgb_ctx;
+
+/* Fill *cfg with the reference namelist defaults for solver_opt = 2 (namelist_n_constants.py:6-54). */
+int lexgb_default_config(lexgb_config *cfg);
+
+/* Create / destroy a solver context (replaces the jit-compiled closure over the
+ * namelist globals that one_sprint_functions.py:9-30 builds). */
+int lexgb_create(const lexgb_config *cfg, lexgb_ctx **out);
+int lexgb_destroy(lexgb_ctx *ctx);
+
+/* Order all of the context's work on this CUDA stream (cudaStream_t passed as void*). */
+int lexgb_set_stream(lexgb_ctx *ctx, void *stream);
+
+/* Base state from the reference's base_state tuple (setup_lex.py:67): horizontally
+ * uniform padded FP64 columns of length nz+2 (theta0, qv0, pi0, rho0). */
+int lexgb_set_base_columns(lexgb_ctx *ctx, const double *theta0, const double *qv0,
+                           const double *pi0, const double *rho0);
+
+/* Hydrostatic base state integrated in FP64 on the GPU from theta0 and qv0 columns
+ * (padded, nz+2) with pi = 1 at z = 0 (setup_lex.py:123-132); pi0 and rho0 are written
+ * back to the optional host columns. */
+int lexgb_integrate_base_state(lexgb_ctx *ctx, const double *theta0, const double *qv0,
+                               double *pi0_out, double *rho0_out);
+
+/* Host <-> device transfer of the six prognostic fields in the reference's padded layout
+ * (dtype LEXGB_F32 or LEXGB_F64); replaces the host/device boundary at jit dispatch
+ * (lex_relay.py:48) and at np.reshape in the writers (write_netcdf.py:56). */
+int lexgb_upload_state(lexgb_ctx *ctx, const void *const fields[6], int dtype);
+int lexgb_download_state(lexgb_ctx *ctx, void *const fields[6], int dtype);
+
+/* Advance nsteps Wicker-Skamarock RK3 big steps (ws_rk3_big_step, one_sprint_functions.py:10-30;
+ * ws_rk3_sprint :109-115 is nsteps = sprint_n).  use_graph != 0 replays a captured CUDA graph
+ * of one big step. */
+int lexgb_step(lexgb_ctx *ctx, int nsteps, int use_graph);
+
+/* One big step that also keeps each stage's output state and the reference's tendency tuple
+ * (d_theta_dt, d_pip_dt, du_dt, dv_dt, dw_dt, d_qv_dt) of rk_sub_step0/1/2
+ * (one_step_integration.py:16-447).  Afterwards lexgb_download_stage() returns them. */
+int lexgb_step_record(lexgb_ctx *ctx);
+/* stage in 0..2; fields (6, padded reference layout) and/or tends (6, interior arrays in
+ * reference C order: theta/pi'/qv (nx,ny,nz), u (nx+1,ny,nz), v (nx,ny+1,nz), w (nx,ny,nz+1)).
+ * Either pointer array may be NULL.  FP64 host output. */
+int lexgb_download_stage(lexgb_ctx *ctx, int stage, double *const fields[6], double *const tends[6]);
+
+/* Single operators evaluated on the current state, for parity checks.  Output is an FP64
+ * host array in the reference's C order for that operator's result. */
+enum {
+    LEXGB_DIAG_MASS_DIV = 0,  /* get_divergence, interior (nx,ny,nz)           advection.py:200 */
+    LEXGB_DIAG_ADV_THETA,     /* advection_scalar(theta), (nx,ny,nz)             advection.py:9 */
+    LEXGB_DIAG_ADV_QV,        /* advection_scalar(qv), (nx,ny,nz)                advection.py:9 */
+    LEXGB_DIAG_ADV_U,         /* advection_u, (nx+1,ny,nz)                       advection.py:37 */
+    LEXGB_DIAG_ADV_V,         /* advection_v, (nx,ny+1,nz)                       advection.py:77 */
+    LEXGB_DIAG_ADV_W,         /* advection_w, (nx,ny,nz+1)                       advection.py:117 */
+    LEXGB_DIAG_BUOY_W,        /* calculate_buoyancy b8w, (nx,ny,nz+1)            pressure_equations.py:162 */
+    LEXGB_DIAG_THETA_RHO,     /* density potential temperature, (nx,ny,nz)       one_step_integration.py:269 */
+    LEXGB_DIAG_PGF_U,         /* pressure_gradient_force, (nx+1,ny,nz)           pressure_gradient_coriolis.py:7 */
+    LEXGB_DIAG_PGF_V,         /* (nx,ny+1,nz) */
+    LEXGB_DIAG_PGF_W,         /* (nx,ny,nz+1) */
+    LEXGB_DIAG_ADV_PI,        /* advection_pi(pi' of the state, winds of the state), (nx,ny,nz) advection.py:152 */
+    LEXGB_DIAG_SGS_U,         /* compute_smag, (nx+1,ny,nz)                      turbulence.py:9 */
+    LEXGB_DIAG_SGS_V,
+    LEXGB_DIAG_SGS_W,
+    LEXGB_DIAG_SGS_THETA,
+    LEXGB_DIAG_SGS_QV,
+    LEXGB_DIAG_N2,            /* compute_nm, interior (nx,ny,nz)                 turbulence.py:391 */
+    LEXGB_DIAG_KM,            /* compute_k km, interior (nx,ny,nz)               turbulence.py:430 */
+    LEXGB_DIAG_COUNT
+};
+int lexgb_diagnose(lexgb_ctx *ctx, int what, double *host_out);
+
+/* FP64 global budgets of the current state (no counterpart in the reference's solver_opt=2
+ * path; space_integration, one_step_integration.py:930-938, is its closest analogue):
+ * out[0] total air mass  sum rho dV (rho from pi0+pi', theta, qv as get_rho, :941-947)
+ * out[1] water vapour mass  sum rho qv dV
+ * out[2] kinetic energy  sum 0.5 rho0 (u^2+v^2+w^2) dV (velocities averaged to cell centres)
+ * out[3] sum rho0 theta dV.  n_out >= 4. */
+int lexgb_budget(lexgb_ctx *ctx, double *out, int n_out);
+
+/* Non-finite check of the state: *n_bad = number of non-finite values (0 = clean). */
+int lexgb_check_finite(lexgb_ctx *ctx, long long *n_bad);
+
+/* Wait for the context's stream. */
+int lexgb_synchronize(lexgb_ctx *ctx);
+
+/* Device pointers of the current state in the internal layout (x fastest, interior only,
+ * theta stored minus theta_ref, u/v periodic without the duplicated face, w with nz+1 levels). */
+int lexgb_state_device_ptrs(lexgb_ctx *ctx, void *ptrs[6]);
+
+/* Message of the last failure on this thread; returns the untruncated length. */
+int lexgb_last_error(char *buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LEXGB_H */

@@ -1,0 +1,637 @@
+// capi.cu - the C ABI of include/lexgb.h: context, device buffers, the Wicker-Skamarock RK3
+// stage driver (one_sprint_functions.py:10-30, one_step_integration.py:16-447), CUDA-graph
+// replay of a big step, host transfers, operator diagnostics and FP64 budgets.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/lexgb.h"
+#include "lexgb_internal.cuh"
+
+using namespace lexgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CK(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      return fail(LEXGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
+  } while (0)
+
+#define CKS(call)                                                                                 \
+  do {                                                                                            \
+    int s_ = (call);                                                                              \
+    if (s_ != LEXGB_OK) return s_;                                                                \
+  } while (0)
+
+constexpr int NFIELD = 6;  // T u v w p q
+
+}  // namespace
+
+struct lexgb_ctx {
+  lexgb_config cfg{};
+  Dims d{};
+  Phys ph{};
+  double theta_ref = 0.0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  size_t fstride = 0;  // floats per field allocation (nx*ny*(nz+1))
+  // FP64 padded base columns theta0 | qv0 | pi0 | rho0 and the FP32 table
+  double* base64 = nullptr;
+  float* tab = nullptr;
+  Cols cols{};
+  bool base_set = false;
+  bool state_set = false;
+  // field arena
+  float* arena = nullptr;
+  size_t arena_fields = 0;
+  State A{}, B{}, C{};
+  float *Xu, *Xv, *Xw, *Xp, *Yu, *Yv, *Yw, *Yp;
+  float *Ru, *Rv, *Rw, *trho, *div;
+  float* sgs[5];
+  float* tau[7];
+  float* diag[3];
+  // record mode (allocated on first use)
+  float* rec_arena = nullptr;
+  State S[3]{}, R0{};
+  float* recdT[3]{};
+  float* recdq[3]{};
+  bool recorded = false;
+  // staging
+  void* stage = nullptr;
+  size_t stage_bytes = 0;
+  double* partial = nullptr;
+  double* budget = nullptr;
+  unsigned long long* count = nullptr;
+  // graph of one big step
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+};
+
+namespace {
+
+State fields_at(float* base, size_t stride) {
+  State s;
+  s.T = base + 0 * stride;
+  s.u = base + 1 * stride;
+  s.v = base + 2 * stride;
+  s.w = base + 3 * stride;
+  s.p = base + 4 * stride;
+  s.q = base + 5 * stride;
+  return s;
+}
+
+float* field_of(const State& s, int f) {
+  switch (f) {
+    case 0: return s.T;
+    case 1: return s.u;
+    case 2: return s.v;
+    case 3: return s.w;
+    case 4: return s.p;
+    default: return s.q;
+  }
+}
+
+int kind_of(int f) { return f == 1 ? 1 : (f == 2 ? 2 : (f == 3 ? 3 : 0)); }
+
+size_t padded_count(const Dims& d, int kind) {
+  return (size_t)(d.nx + 6 + (kind == 1)) * (d.ny + 6 + (kind == 2)) * (d.nz + 2 + (kind == 3));
+}
+
+size_t interior_count(const Dims& d, int kind) {
+  return (size_t)(d.nx + (kind == 1)) * (d.ny + (kind == 2)) * (d.nz + (kind == 3));
+}
+
+struct StagePlan {
+  double dts[3];
+  int n[3];
+  double dtau[3];
+};
+
+// one_sprint_functions.py:19-21 and one_step_integration.py:121-122, :253-254
+StagePlan plan_of(const lexgb_config& c) {
+  StagePlan p;
+  const double dt_sound = c.dt / c.n_sound;
+  p.dts[0] = c.dt / 3.0;
+  p.dts[1] = c.dt / 2.0;
+  p.dts[2] = c.dt;
+  p.n[0] = 1;
+  p.dtau[0] = p.dts[0];
+  p.n[1] = (int)lround(p.dts[1] / dt_sound);
+  p.n[2] = (int)lround(p.dts[2] / dt_sound);
+  p.dtau[1] = p.dtau[2] = dt_sound;
+  return p;
+}
+
+int run_smag(lexgb_ctx* c, const State& x, float* n2, float* km) {
+  SmagTau t{c->tau[0], c->tau[1], c->tau[2], c->tau[3], c->tau[4], c->tau[5], c->tau[6], n2, km};
+  CK(launch_smag_a(c->d, c->ph, c->cols, x, t, c->stream));
+  SgsOut o{c->sgs[0], c->sgs[1], c->sgs[2], c->sgs[3], c->sgs[4]};
+  CK(launch_smag_b(c->d, c->ph, c->cols, x, t, o, c->stream));
+  return LEXGB_OK;
+}
+
+// One WS-RK3 stage: xi_out = xi0 + dts * F(xis) (rk_sub_step0/1/2 with solver_opt = 2).
+int run_stage(lexgb_ctx* c, int s, const State& xi0, const State& xis, const State& out, float* dT, float* dq) {
+  const StagePlan p = plan_of(c->cfg);
+  const bool sgs_on = c->cfg.turb_opt == 1;
+  CK(launch_div_trho(c->d, c->ph, c->cols, xis, c->div, c->trho, c->stream));
+  Sgs sg{nullptr, nullptr, nullptr, nullptr, nullptr};
+  if (sgs_on) sg = Sgs{c->sgs[0], c->sgs[1], c->sgs[2], c->sgs[3], c->sgs[4]};
+  SlowOut so{nullptr, nullptr, nullptr, out.T, out.q, dT, dq};
+  CK(launch_adv_scalars(c->d, c->ph, c->cols, xis, c->div, xi0.T, xi0.q, sg, (float)p.dts[s], so, c->stream));
+  CK(launch_adv_u(c->d, c->ph, c->cols, xis, c->div, sg.u, c->Ru, c->stream));
+  CK(launch_adv_v(c->d, c->ph, c->cols, xis, c->div, sg.v, c->Rv, c->stream));
+  CK(launch_adv_w(c->d, c->ph, c->cols, xis, c->div, sg.w, c->Rw, 0, c->stream));
+  // acoustic sub-steps from xi0's winds and pi'; pi'_s is the stage state's pi'
+  const int n = p.n[s];
+  const float dtau = (float)p.dtau[s];
+  AcousticIn in{xi0.u, xi0.v, xi0.w, xi0.p, c->Ru, c->Rv, c->Rw, c->trho, xis.p};
+  const AcousticOut X{c->Xu, c->Xv, c->Xw, c->Xp}, Y{c->Yu, c->Yv, c->Yw, c->Yp};
+  const AcousticOut O{out.u, out.v, out.w, out.p};
+  const bool alias = (out.u == xi0.u);
+  for (int m = 1; m <= n; ++m) {
+    AcousticOut tgt = (m == n && !(alias && n == 1)) ? O : ((m & 1) ? X : Y);
+    CK(launch_acoustic(c->d, c->ph, c->cols, in, tgt, dtau, c->stream));
+    in.u = tgt.u;
+    in.v = tgt.v;
+    in.w = tgt.w;
+    in.p = tgt.p;
+  }
+  if (alias && n == 1) {  // single sub-step into the buffer it started from: stage through X
+    const size_t bytes = c->fstride * sizeof(float);
+    CK(cudaMemcpyAsync(out.u, c->Xu, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(out.v, c->Xv, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(out.w, c->Xw, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(out.p, c->Xp, bytes, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  return LEXGB_OK;
+}
+
+// One big step A -> A (stage 0: A -> B, stage 1: B -> C, stage 2: C -> A in place).
+int run_step(lexgb_ctx* c) {
+  if (c->cfg.turb_opt == 1) CKS(run_smag(c, c->A, nullptr, nullptr));
+  CKS(run_stage(c, 0, c->A, c->A, c->B, nullptr, nullptr));
+  CKS(run_stage(c, 1, c->A, c->B, c->C, nullptr, nullptr));
+  CKS(run_stage(c, 2, c->A, c->C, c->A, nullptr, nullptr));
+  return LEXGB_OK;
+}
+
+int ensure_record(lexgb_ctx* c) {
+  if (c->rec_arena) return LEXGB_OK;
+  const size_t nf = 4 * NFIELD + 6;
+  cudaError_t e = cudaMalloc(&c->rec_arena, nf * c->fstride * sizeof(float));
+  if (e != cudaSuccess) return fail(LEXGB_ERR_ALLOC, std::string("record buffers: ") + cudaGetErrorString(e));
+  for (int s = 0; s < 3; ++s) c->S[s] = fields_at(c->rec_arena + (size_t)s * NFIELD * c->fstride, c->fstride);
+  c->R0 = fields_at(c->rec_arena + (size_t)3 * NFIELD * c->fstride, c->fstride);
+  float* t = c->rec_arena + (size_t)4 * NFIELD * c->fstride;
+  for (int s = 0; s < 3; ++s) {
+    c->recdT[s] = t + (size_t)(2 * s) * c->fstride;
+    c->recdq[s] = t + (size_t)(2 * s + 1) * c->fstride;
+  }
+  return LEXGB_OK;
+}
+
+int copy_state(lexgb_ctx* c, const State& dst, const State& src) {
+  for (int f = 0; f < NFIELD; ++f)
+    CK(cudaMemcpyAsync(field_of(dst, f), field_of(src, f), c->fstride * sizeof(float), cudaMemcpyDeviceToDevice,
+                       c->stream));
+  return LEXGB_OK;
+}
+
+int check_ready(lexgb_ctx* c) {
+  if (!c) return fail(LEXGB_ERR_ARG, "null context");
+  if (!c->base_set) return fail(LEXGB_ERR_STATE, "base state not set (lexgb_set_base_columns / lexgb_integrate_base_state)");
+  if (!c->state_set) return fail(LEXGB_ERR_STATE, "prognostic state not uploaded (lexgb_upload_state)");
+  return LEXGB_OK;
+}
+
+int ensure_stage(lexgb_ctx* c, size_t bytes) {
+  if (c->stage_bytes >= bytes) return LEXGB_OK;
+  if (c->stage) cudaFree(c->stage);
+  c->stage = nullptr;
+  c->stage_bytes = 0;
+  cudaError_t e = cudaMalloc(&c->stage, bytes);
+  if (e != cudaSuccess) return fail(LEXGB_ERR_ALLOC, std::string("staging buffer: ") + cudaGetErrorString(e));
+  c->stage_bytes = bytes;
+  return LEXGB_OK;
+}
+
+void drop_graph(lexgb_ctx* c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->gexec = nullptr;
+  c->graph = nullptr;
+}
+
+int build_table(lexgb_ctx* c) {
+  const int nz = c->d.nz;
+  double th1 = 0.0;
+  CK(cudaMemcpyAsync(&th1, c->base64 + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->theta_ref = c->cfg.theta_ref != 0.0 ? c->cfg.theta_ref : th1;
+  c->ph.theta_ref = (float)c->theta_ref;
+  if ((double)c->ph.theta_ref != c->theta_ref)
+    return fail(LEXGB_ERR_ARG, "theta_ref must be exactly representable in FP32");
+  const size_t S = nz + 2;
+  CK(launch_build_columns(nz, c->cfg.dz, c->theta_ref, c->base64, c->base64 + S, c->base64 + 2 * S,
+                          c->base64 + 3 * S, c->tab, c->stream));
+  float* t = c->tab;
+  c->cols = Cols{t, t + S, t + 2 * S, t + 3 * S, t + 4 * S, t + 5 * S, t + 6 * S, t + 7 * S, t + 8 * S, t + 9 * S};
+  c->base_set = true;
+  drop_graph(c);
+  return LEXGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lexgb_default_config(lexgb_config* cfg) {
+  if (!cfg) return fail(LEXGB_ERR_ARG, "null config");
+  memset(cfg, 0, sizeof(*cfg));
+  cfg->nx = 240;  // namelist_n_constants.py:20-22
+  cfg->ny = 240;
+  cfg->nz = 120;
+  cfg->dx = cfg->dy = cfg->dz = 100.0;
+  cfg->dt = 1.0;
+  cfg->n_sound = 32;
+  cfg->turb_opt = 0;
+  cfg->cor_opt = 0;
+  cfg->f_cor = 1.0e-4;
+  cfg->theta_ref = 0.0;
+  return LEXGB_OK;
+}
+
+int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
+  if (!cfg || !out) return fail(LEXGB_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (cfg->nx < 4 || cfg->ny < 4 || cfg->nz < 6)
+    return fail(LEXGB_ERR_ARG, "grid too small: need nx, ny >= 4 and nz >= 6");
+  if ((long long)cfg->nx * cfg->ny * (cfg->nz + 1) >= (1LL << 31))
+    return fail(LEXGB_ERR_ARG, "grid too large: nx*ny*(nz+1) must be < 2^31");
+  if (!(cfg->dx > 0) || !(cfg->dy > 0) || !(cfg->dz > 0) || !(cfg->dt > 0))
+    return fail(LEXGB_ERR_ARG, "dx, dy, dz and dt must be positive");
+  if (cfg->n_sound < 1) return fail(LEXGB_ERR_ARG, "n_sound must be >= 1");
+  if (cfg->turb_opt != 0 && cfg->turb_opt != 1)
+    return fail(LEXGB_ERR_ARG, "turb_opt must be 0 or 1 (the anisotropic turb_opt=2 is not provided)");
+  if (cfg->cor_opt < 0 || cfg->cor_opt > 2) return fail(LEXGB_ERR_ARG, "cor_opt must be 0, 1 or 2");
+  lexgb_ctx* c = new lexgb_ctx();
+  c->cfg = *cfg;
+  c->d = Dims{cfg->nx, cfg->ny, cfg->nz};
+  c->ph.dx = (float)cfg->dx;
+  c->ph.dy = (float)cfg->dy;
+  c->ph.dz = (float)cfg->dz;
+  c->ph.rdx = (float)(1.0 / cfg->dx);
+  c->ph.rdy = (float)(1.0 / cfg->dy);
+  c->ph.rdz = (float)(1.0 / cfg->dz);
+  const double l = kCs * cbrt(cfg->dx * cfg->dy * cfg->dz);
+  c->ph.smag_l2 = (float)(l * l);
+  c->ph.cor_opt = cfg->cor_opt;
+  c->ph.f_cor = (float)cfg->f_cor;
+  c->fstride = (size_t)cfg->nx * cfg->ny * (cfg->nz + 1);
+  c->fstride = (c->fstride + 63) / 64 * 64;  // 256-byte aligned fields
+  auto bail = [&](int code, const std::string& m) {
+    lexgb_destroy(c);
+    return fail(code, m);
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
+  c->stream = c->own_stream;
+  // 3 states + 2 acoustic ping-pong sets + R(3) + trho + div + sgs(5) + tau(7) + diag(3)
+  c->arena_fields = 3 * NFIELD + 8 + 5 + 5 + 7 + 3;
+  e = cudaMalloc(&c->arena, c->arena_fields * c->fstride * sizeof(float));
+  if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("field arena: ") + cudaGetErrorString(e));
+  e = cudaMemsetAsync(c->arena, 0, c->arena_fields * c->fstride * sizeof(float), c->stream);
+  if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e));
+  float* p = c->arena;
+  auto take = [&]() {
+    float* r = p;
+    p += c->fstride;
+    return r;
+  };
+  c->A = fields_at(take(), c->fstride);
+  for (int i = 0; i < NFIELD - 1; ++i) take();
+  c->B = fields_at(take(), c->fstride);
+  for (int i = 0; i < NFIELD - 1; ++i) take();
+  c->C = fields_at(take(), c->fstride);
+  for (int i = 0; i < NFIELD - 1; ++i) take();
+  c->Xu = take(); c->Xv = take(); c->Xw = take(); c->Xp = take();
+  c->Yu = take(); c->Yv = take(); c->Yw = take(); c->Yp = take();
+  c->Ru = take(); c->Rv = take(); c->Rw = take(); c->trho = take(); c->div = take();
+  for (int i = 0; i < 5; ++i) c->sgs[i] = take();
+  for (int i = 0; i < 7; ++i) c->tau[i] = take();
+  for (int i = 0; i < 3; ++i) c->diag[i] = take();
+  e = cudaMalloc(&c->base64, 4 * (cfg->nz + 2) * sizeof(double));
+  if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("base columns: ") + cudaGetErrorString(e));
+  e = cudaMalloc(&c->tab, 10 * (cfg->nz + 2) * sizeof(float));
+  if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("column table: ") + cudaGetErrorString(e));
+  e = cudaMalloc(&c->partial, (size_t)budget_blocks(c->d) * 4 * sizeof(double));
+  if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("budget partials: ") + cudaGetErrorString(e));
+  e = cudaMalloc(&c->budget, 4 * sizeof(double));
+  if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("budget: ") + cudaGetErrorString(e));
+  e = cudaMalloc(&c->count, sizeof(unsigned long long));
+  if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("counter: ") + cudaGetErrorString(e));
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
+  *out = c;
+  return LEXGB_OK;
+}
+
+int lexgb_destroy(lexgb_ctx* c) {
+  if (!c) return LEXGB_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  drop_graph(c);
+  cudaFree(c->arena);
+  cudaFree(c->rec_arena);
+  cudaFree(c->base64);
+  cudaFree(c->tab);
+  cudaFree(c->stage);
+  cudaFree(c->partial);
+  cudaFree(c->budget);
+  cudaFree(c->count);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return LEXGB_OK;
+}
+
+int lexgb_set_stream(lexgb_ctx* c, void* stream) {
+  if (!c) return fail(LEXGB_ERR_ARG, "null context");
+  CK(cudaStreamSynchronize(c->stream));
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  drop_graph(c);
+  return LEXGB_OK;
+}
+
+int lexgb_set_base_columns(lexgb_ctx* c, const double* theta0, const double* qv0, const double* pi0,
+                           const double* rho0) {
+  if (!c || !theta0 || !qv0 || !pi0 || !rho0) return fail(LEXGB_ERR_ARG, "null argument");
+  const size_t S = c->d.nz + 2;
+  for (size_t k = 0; k < S; ++k)
+    if (!(theta0[k] > 0) || !(rho0[k] > 0) || !(pi0[k] > 0) || !isfinite(qv0[k]))
+      return fail(LEXGB_ERR_ARG, "base columns must be finite with positive theta0, pi0, rho0");
+  const double* src[4] = {theta0, qv0, pi0, rho0};
+  for (int a = 0; a < 4; ++a)
+    CK(cudaMemcpyAsync(c->base64 + a * S, src[a], S * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  return build_table(c);
+}
+
+int lexgb_integrate_base_state(lexgb_ctx* c, const double* theta0, const double* qv0, double* pi0_out,
+                               double* rho0_out) {
+  if (!c || !theta0 || !qv0) return fail(LEXGB_ERR_ARG, "null argument");
+  const size_t S = c->d.nz + 2;
+  CK(cudaMemcpyAsync(c->base64, theta0, S * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->base64 + S, qv0, S * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(launch_hydrostatic(c->d.nz, c->cfg.dz, c->base64, c->base64 + S, c->base64 + 2 * S, c->base64 + 3 * S,
+                        c->stream));
+  CKS(build_table(c));
+  if (pi0_out)
+    CK(cudaMemcpyAsync(pi0_out, c->base64 + 2 * S, S * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (rho0_out)
+    CK(cudaMemcpyAsync(rho0_out, c->base64 + 3 * S, S * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return LEXGB_OK;
+}
+
+int lexgb_upload_state(lexgb_ctx* c, const void* const fields[6], int dtype) {
+  if (!c || !fields) return fail(LEXGB_ERR_ARG, "null argument");
+  if (dtype != LEXGB_F32 && dtype != LEXGB_F64) return fail(LEXGB_ERR_ARG, "dtype must be LEXGB_F32 or LEXGB_F64");
+  if (!c->base_set) return fail(LEXGB_ERR_STATE, "set the base state before uploading (theta_ref comes from it)");
+  const size_t esz = dtype == LEXGB_F64 ? 8 : 4;
+  size_t off[NFIELD + 1] = {0};
+  for (int f = 0; f < NFIELD; ++f) {
+    if (!fields[f]) return fail(LEXGB_ERR_ARG, "null field pointer");
+    off[f + 1] = off[f] + (padded_count(c->d, kind_of(f)) * esz + 255) / 256 * 256;
+  }
+  CKS(ensure_stage(c, off[NFIELD]));
+  for (int f = 0; f < NFIELD; ++f) {
+    char* dst = (char*)c->stage + off[f];
+    CK(cudaMemcpyAsync(dst, fields[f], padded_count(c->d, kind_of(f)) * esz, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_import_padded(c->d, dst, dtype == LEXGB_F64, kind_of(f), f == 0 ? c->theta_ref : 0.0,
+                            field_of(c->A, f), c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  c->state_set = true;
+  c->recorded = false;
+  return LEXGB_OK;
+}
+
+int lexgb_download_state(lexgb_ctx* c, void* const fields[6], int dtype) {
+  CKS(check_ready(c));
+  if (!fields) return fail(LEXGB_ERR_ARG, "null argument");
+  if (dtype != LEXGB_F32 && dtype != LEXGB_F64) return fail(LEXGB_ERR_ARG, "dtype must be LEXGB_F32 or LEXGB_F64");
+  const size_t esz = dtype == LEXGB_F64 ? 8 : 4;
+  size_t off[NFIELD + 1] = {0};
+  for (int f = 0; f < NFIELD; ++f) off[f + 1] = off[f] + (padded_count(c->d, kind_of(f)) * esz + 255) / 256 * 256;
+  CKS(ensure_stage(c, off[NFIELD]));
+  for (int f = 0; f < NFIELD; ++f) {
+    if (!fields[f]) continue;
+    char* src = (char*)c->stage + off[f];
+    CK(launch_export_padded(c->d, field_of(c->A, f), kind_of(f), f == 0 ? c->theta_ref : 0.0, src,
+                            dtype == LEXGB_F64, c->stream));
+    CK(cudaMemcpyAsync(fields[f], src, padded_count(c->d, kind_of(f)) * esz, cudaMemcpyDeviceToHost, c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return LEXGB_OK;
+}
+
+int lexgb_step(lexgb_ctx* c, int nsteps, int use_graph) {
+  CKS(check_ready(c));
+  if (nsteps < 0) return fail(LEXGB_ERR_ARG, "nsteps must be >= 0");
+  c->recorded = false;
+  if (!use_graph) {
+    for (int n = 0; n < nsteps; ++n) CKS(run_step(c));
+    return LEXGB_OK;
+  }
+  if (!c->gexec) {
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const int st = run_step(c);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (st != LEXGB_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (e != cudaSuccess) return fail(LEXGB_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    c->graph = g;
+    CK(cudaGraphInstantiate(&c->gexec, c->graph, 0));
+  }
+  for (int n = 0; n < nsteps; ++n) CK(cudaGraphLaunch(c->gexec, c->stream));
+  return LEXGB_OK;
+}
+
+int lexgb_step_record(lexgb_ctx* c) {
+  CKS(check_ready(c));
+  CKS(ensure_record(c));
+  CKS(copy_state(c, c->R0, c->A));
+  if (c->cfg.turb_opt == 1) CKS(run_smag(c, c->A, nullptr, nullptr));
+  CKS(run_stage(c, 0, c->A, c->A, c->S[0], c->recdT[0], c->recdq[0]));
+  CKS(run_stage(c, 1, c->A, c->S[0], c->S[1], c->recdT[1], c->recdq[1]));
+  CKS(run_stage(c, 2, c->A, c->S[1], c->S[2], c->recdT[2], c->recdq[2]));
+  CKS(copy_state(c, c->A, c->S[2]));
+  CK(cudaStreamSynchronize(c->stream));
+  c->recorded = true;
+  return LEXGB_OK;
+}
+
+int lexgb_download_stage(lexgb_ctx* c, int stage, double* const fields[6], double* const tends[6]) {
+  CKS(check_ready(c));
+  if (!c->recorded) return fail(LEXGB_ERR_STATE, "no recorded step (call lexgb_step_record first)");
+  if (stage < 0 || stage > 2) return fail(LEXGB_ERR_ARG, "stage must be 0, 1 or 2");
+  const StagePlan p = plan_of(c->cfg);
+  size_t maxp = 0;
+  for (int f = 0; f < NFIELD; ++f) maxp = padded_count(c->d, kind_of(f)) > maxp ? padded_count(c->d, kind_of(f)) : maxp;
+  CKS(ensure_stage(c, 2 * maxp * sizeof(double)));
+  double* s0 = (double*)c->stage;
+  double* s1 = s0 + maxp;
+  std::vector<double> h0, h1;
+  for (int f = 0; f < NFIELD; ++f) {
+    const int kd = kind_of(f);
+    const double off = f == 0 ? c->theta_ref : 0.0;
+    if (fields && fields[f]) {
+      CK(launch_export_padded(c->d, field_of(c->S[stage], f), kd, off, s0, 1, c->stream));
+      CK(cudaMemcpyAsync(fields[f], s0, padded_count(c->d, kd) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+    }
+    if (!tends || !tends[f]) continue;
+    const size_t n = interior_count(c->d, kd);
+    if (f == 0 || f == 5) {  // d_theta_dt / d_qv_dt recorded by the scalar kernel
+      CK(launch_export_interior(c->d, f == 0 ? c->recdT[stage] : c->recdq[stage], kd, 0.0, s0, c->stream));
+      CK(cudaMemcpyAsync(tends[f], s0, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+    } else {  // (x_stage - x0) / dt_stage, one_step_integration.py:157-160
+      CK(launch_export_interior(c->d, field_of(c->S[stage], f), kd, 0.0, s0, c->stream));
+      CK(launch_export_interior(c->d, field_of(c->R0, f), kd, 0.0, s1, c->stream));
+      h0.resize(n);
+      h1.resize(n);
+      CK(cudaMemcpyAsync(h0.data(), s0, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaMemcpyAsync(h1.data(), s1, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      CK(cudaStreamSynchronize(c->stream));
+      for (size_t t = 0; t < n; ++t) tends[f][t] = (h0[t] - h1[t]) / p.dts[stage];
+    }
+  }
+  return LEXGB_OK;
+}
+
+int lexgb_diagnose(lexgb_ctx* c, int what, double* host_out) {
+  CKS(check_ready(c));
+  if (!host_out) return fail(LEXGB_ERR_ARG, "null output");
+  if (what < 0 || what >= LEXGB_DIAG_COUNT) return fail(LEXGB_ERR_ARG, "unknown diagnostic");
+  const Dims& d = c->d;
+  Phys ph = c->ph;
+  ph.cor_opt = 0;  // pure advection
+  float* out = c->diag[0];
+  int kind = 0;
+  CK(launch_div_trho(d, ph, c->cols, c->A, c->div, c->trho, c->stream));
+  const Sgs none{nullptr, nullptr, nullptr, nullptr, nullptr};
+  switch (what) {
+    case LEXGB_DIAG_MASS_DIV: out = c->div; break;
+    case LEXGB_DIAG_THETA_RHO: out = c->trho; break;
+    case LEXGB_DIAG_ADV_THETA:
+    case LEXGB_DIAG_ADV_QV: {
+      SlowOut so{nullptr, nullptr, nullptr, nullptr, nullptr, c->diag[0], c->diag[1]};
+      CK(launch_adv_scalars(d, ph, c->cols, c->A, c->div, c->A.T, c->A.q, none, 0.f, so, c->stream));
+      out = what == LEXGB_DIAG_ADV_THETA ? c->diag[0] : c->diag[1];
+      break;
+    }
+    case LEXGB_DIAG_ADV_U: CK(launch_adv_u(d, ph, c->cols, c->A, c->div, nullptr, out, c->stream)); kind = 1; break;
+    case LEXGB_DIAG_ADV_V: CK(launch_adv_v(d, ph, c->cols, c->A, c->div, nullptr, out, c->stream)); kind = 2; break;
+    case LEXGB_DIAG_ADV_W: CK(launch_adv_w(d, ph, c->cols, c->A, c->div, nullptr, out, 1, c->stream)); kind = 3; break;
+    case LEXGB_DIAG_BUOY_W: CK(launch_adv_w(d, ph, c->cols, c->A, c->div, nullptr, out, 2, c->stream)); kind = 3; break;
+    case LEXGB_DIAG_PGF_U:
+    case LEXGB_DIAG_PGF_V:
+    case LEXGB_DIAG_PGF_W:
+      CK(launch_diag_pgf(d, ph, c->cols, c->A.p, c->trho, c->diag[0], c->diag[1], c->diag[2], c->stream));
+      kind = what - LEXGB_DIAG_PGF_U + 1;
+      out = c->diag[what - LEXGB_DIAG_PGF_U];
+      break;
+    case LEXGB_DIAG_ADV_PI:
+      CK(launch_diag_advpi(d, ph, c->cols, c->A.p, c->A.u, c->A.v, c->A.w, out, c->stream));
+      break;
+    case LEXGB_DIAG_SGS_U:
+    case LEXGB_DIAG_SGS_V:
+    case LEXGB_DIAG_SGS_W:
+    case LEXGB_DIAG_SGS_THETA:
+    case LEXGB_DIAG_SGS_QV:
+    case LEXGB_DIAG_N2:
+    case LEXGB_DIAG_KM: {
+      CKS(run_smag(c, c->A, c->diag[1], c->diag[2]));
+      if (what == LEXGB_DIAG_N2) {
+        out = c->diag[1];
+      } else if (what == LEXGB_DIAG_KM) {
+        out = c->diag[2];
+      } else {
+        const int m = what - LEXGB_DIAG_SGS_U;
+        out = c->sgs[m];
+        kind = m < 3 ? m + 1 : 0;
+      }
+      break;
+    }
+    default: return fail(LEXGB_ERR_ARG, "unknown diagnostic");
+  }
+  const size_t n = interior_count(d, kind);
+  CKS(ensure_stage(c, n * sizeof(double)));
+  CK(launch_export_interior(d, out, kind, 0.0, (double*)c->stage, c->stream));
+  CK(cudaMemcpyAsync(host_out, c->stage, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return LEXGB_OK;
+}
+
+int lexgb_budget(lexgb_ctx* c, double* out, int n_out) {
+  CKS(check_ready(c));
+  if (!out || n_out < 4) return fail(LEXGB_ERR_ARG, "budget needs an output array of at least 4 doubles");
+  const size_t S = c->d.nz + 2;
+  CK(launch_budget(c->d, c->ph, c->cols, c->A, c->base64 + 3 * S, c->base64 + 2 * S, c->theta_ref, c->partial,
+                   c->budget, c->stream));
+  CK(cudaMemcpyAsync(out, c->budget, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return LEXGB_OK;
+}
+
+int lexgb_check_finite(lexgb_ctx* c, long long* n_bad) {
+  CKS(check_ready(c));
+  if (!n_bad) return fail(LEXGB_ERR_ARG, "null output");
+  CK(cudaMemsetAsync(c->count, 0, sizeof(unsigned long long), c->stream));
+  for (int f = 0; f < NFIELD; ++f)
+    CK(launch_count_nonfinite(field_of(c->A, f), f == 3 ? c->d.faces() : c->d.cells(), c->count, c->stream));
+  unsigned long long h = 0;
+  CK(cudaMemcpyAsync(&h, c->count, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *n_bad = (long long)h;
+  return LEXGB_OK;
+}
+
+int lexgb_synchronize(lexgb_ctx* c) {
+  if (!c) return fail(LEXGB_ERR_ARG, "null context");
+  CK(cudaStreamSynchronize(c->stream));
+  return LEXGB_OK;
+}
+
+int lexgb_state_device_ptrs(lexgb_ctx* c, void* ptrs[6]) {
+  if (!c || !ptrs) return fail(LEXGB_ERR_ARG, "null argument");
+  for (int f = 0; f < NFIELD; ++f) ptrs[f] = field_of(c->A, f);
+  return LEXGB_OK;
+}
+
+int lexgb_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    const size_t n = g_last_error.size() < len - 1 ? g_last_error.size() : len - 1;
+    memcpy(buf, g_last_error.data(), n);
+    buf[n] = '\0';
+  }
+  return (int)g_last_error.size();
+}
+
+}  // extern "C"

@@ -1,0 +1,236 @@
+// lexgb_internal.cuh - device layout, shared reconstruction/physics helpers and kernel
+// launchers of the lex_gb300 dynamical core.
+//
+// Device layout
+//   Every field is stored interior-only, x fastest: idx(i, j, k) = (k*ny + j)*nx + i.
+//   theta, pi', qv, u, v have nz levels; w has nz+1 levels (faces 0..nz, w = 0 at 0 and nz).
+//   u(i) sits on the west face of cell i and v(j) on the south face of cell j; the
+//   reference's duplicated periodic face u[nx] (== u[0]) is not stored
+//   (padding3u_array, one_step_integration.py:962-972).
+//   Lateral halos are periodic and realised by index wrap; the reference's z ghost levels
+//   (edge copies, one_step_integration.py:950-959) by clamping.
+//   theta is stored as T = theta - theta_ref (theta_ref a constant): every operator on
+//   theta is either affine-invariant (WENO reconstructions, flux form + theta*div,
+//   gradients) or is rewritten exactly in terms of T, which keeps FP32 increments of a
+//   ~300 K field representable.
+//
+// Base state
+//   Horizontally uniform; kept as FP32 per-level columns derived in FP64 on the device
+//   (Cols below).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lexgb {
+
+// namelist_n_constants.py:64-75, evaluated in double and rounded once
+constexpr double kRd = 287.04;
+constexpr double kRv = 461.5;
+constexpr double kCp = 1004.64;
+constexpr double kCv = kCp - kRd;
+constexpr double kG = 9.80616;
+constexpr double kP00 = 100000.0;
+constexpr double kReps = kRv / kRd;
+constexpr double kRepsm1 = kRv / kRd - 1.0;
+
+constexpr float kWepsMom = 1.0e-16f;    // one_step_integration.py:896
+constexpr float kWepsTheta = 1.0e-17f;  // one_step_integration.py:905
+constexpr float kWepsQv = 1.0e-18f;     // one_step_integration.py:913
+constexpr float kDivDamp = 1.1f;        // one_step_integration.py:546
+constexpr double kPrandtl = 1.0 / 3.0;  // turbulence.py:432
+constexpr double kCs = 0.18;            // turbulence.py:433
+// fmin(1e30, .) of the reference (advection.py:322) would square to inf in FP32; the cap
+// below keeps every weight finite.  It only differs from the reference where a ratio
+// exceeds 1e18, where the capped weight already dominates the normalised sum.
+constexpr float kRatioCap = 1.0e18f;
+
+struct Dims {
+  int nx, ny, nz;
+  __host__ __device__ __forceinline__ int plane() const { return nx * ny; }
+  __host__ __device__ __forceinline__ int at(int i, int j, int k) const { return (k * ny + j) * nx + i; }
+  __host__ __device__ __forceinline__ long long cells() const { return (long long)nx * ny * nz; }
+  __host__ __device__ __forceinline__ long long faces() const { return (long long)nx * ny * (nz + 1); }
+};
+
+// FP32 base-state columns (device pointers into one allocation).
+struct Cols {
+  const float* rho;       // nz    rho0 at cells
+  const float* rho_face;  // nz+1  0.5*(rho0_pad[f] + rho0_pad[f+1]) (ghost levels at the ends)
+  const float* rho_face0; // nz+1  same with 0 at f = 0 and f = nz (get_divergence, advection.py:213-215)
+  const float* rho_wext;  // nz+1  interpolate_scalar2w(rho0) (pressure_equations.py:123)
+  const float* theta0;    // nz
+  const float* qv0;       // nz
+  const float* trho0;     // nz    theta0*(1+reps*qv0)/(1+qv0)
+  const float* d0;        // nz    theta0 - theta_ref
+  const float* pi0;       // nz
+  const float* dpi0dz;    // nz+1  (pi0_pad[f+1] - pi0_pad[f]) / dz
+};
+
+struct Phys {
+  float dx, dy, dz;
+  float rdx, rdy, rdz;
+  float theta_ref;
+  float smag_l2;  // (Cs * cbrt(dx dy dz))^2
+  int cor_opt;
+  float f_cor;
+};
+
+__device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+__device__ __forceinline__ int clampi(int i, int lo, int hi) { return i < lo ? lo : (i > hi ? hi : i); }
+
+// ---------------------------------------------------------------------------------------------
+// reconstruction (advection.py:305-416 and the lateral blocks :424-503)
+// ---------------------------------------------------------------------------------------------
+// WENO5 value at the face right of c; a..e ordered upwind -> downwind.
+__device__ __forceinline__ float weno5(float a, float b, float c, float d, float e, float eps) {
+  const float t1 = a - 2.f * b + c, t2 = a - 4.f * b + 3.f * c;
+  const float t3 = b - 2.f * c + d, t4 = b - d;
+  const float t5 = c - 2.f * d + e, t6 = 3.f * c - 4.f * d + e;
+  const float b1 = (13.f / 12.f) * t1 * t1 + 0.25f * t2 * t2;
+  const float b2 = (13.f / 12.f) * t3 * t3 + 0.25f * t4 * t4;
+  const float b3 = (13.f / 12.f) * t5 * t5 + 0.25f * t6 * t6;
+  const float tau = fabsf(b1 - b3);
+  const float r1 = fminf(kRatioCap, __fdividef(tau, b1 + eps));
+  const float r2 = fminf(kRatioCap, __fdividef(tau, b2 + eps));
+  const float r3 = fminf(kRatioCap, __fdividef(tau, b3 + eps));
+  const float w1 = 0.1f * (1.f + r1 * r1);
+  const float w2 = 0.6f * (1.f + r2 * r2);
+  const float w3 = 0.3f * (1.f + r3 * r3);
+  const float q1 = (2.f / 6.f) * a + (-7.f / 6.f) * b + (11.f / 6.f) * c;
+  const float q2 = (-1.f / 6.f) * b + (5.f / 6.f) * c + (2.f / 6.f) * d;
+  const float q3 = (2.f / 6.f) * c + (5.f / 6.f) * d + (-1.f / 6.f) * e;
+  return __fdividef(w1 * q1 + w2 * q2 + w3 * q3, w1 + w2 + w3);
+}
+
+// WENO3 value at the face right of b; a, b, c = s[-1], s[0], s[+1] upwind-ordered.
+__device__ __forceinline__ float weno3(float a, float b, float c, float eps) {
+  const float b1 = (a - b) * (a - b);
+  const float b2 = (b - c) * (b - c);
+  const float tau = fabsf(b1 - b2);
+  const float r1 = fminf(kRatioCap, __fdividef(tau, b1 + eps));
+  const float r2 = fminf(kRatioCap, __fdividef(tau, b2 + eps));
+  const float w1 = (1.f / 3.f) * (1.f + r1 * r1);
+  const float w2 = (2.f / 3.f) * (1.f + r2 * r2);
+  return __fdividef(w1 * (-0.5f * a + 1.5f * b) + w2 * (0.5f * b + 0.5f * c), w1 + w2);
+}
+
+// Vertical face value between column entries f-1 and f of an n-entry column s(0..n-1),
+// for upward (m >= 0) or downward flow; zero at f = 0 and f = n.  Centred / WENO3 next to
+// the ends exactly as vertical_flux_scalar2 / _u2 / _v2 / _w2 do.
+template <class F>
+__device__ __forceinline__ float vrecon(const F& s, int f, int n, bool up, float eps) {
+  if (f <= 0 || f >= n) return 0.f;
+  if (up) {
+    if (f == 1) return 0.5f * (s(0) + s(1));
+    if (f == 2) return weno3(s(0), s(1), s(2), eps);
+    if (f == n - 1) return weno3(s(n - 3), s(n - 2), s(n - 1), eps);
+    return weno5(s(f - 3), s(f - 2), s(f - 1), s(f), s(f + 1), eps);
+  } else {
+    if (f == 1) return weno3(s(2), s(1), s(0), eps);
+    if (f == n - 1) return 0.5f * (s(n - 1) + s(n - 2));
+    if (f == n - 2) return weno3(s(n - 1), s(n - 2), s(n - 3), eps);
+    return weno5(s(f + 2), s(f + 1), s(f), s(f - 1), s(f - 2), eps);
+  }
+}
+
+// jax.lax.select(m >= 0, m*pos, m*neg): ties take the positive branch.
+__device__ __forceinline__ float upwind(float m, float pos, float neg) { return m >= 0.f ? m * pos : m * neg; }
+
+// ---------------------------------------------------------------------------------------------
+// thermodynamics
+// ---------------------------------------------------------------------------------------------
+// density potential temperature theta*(1+reps*qv)/(1+qv) (one_step_integration.py:269)
+__device__ __forceinline__ float theta_rho(float T, float q, float theta_ref) {
+  return (theta_ref + T) * (1.f + (float)kReps * q) / (1.f + q);
+}
+
+// g*(theta_rho - theta_rho0)/theta_rho0 (pressure_equations.py:162-172), with
+// theta_rho - theta_rho0 = [theta0 (reps-1)(q - q0) + (theta - theta0)(1 + reps q)(1 + q0)] / ((1+q)(1+q0))
+// evaluated from T = theta - theta_ref and d0 = theta0 - theta_ref.
+__device__ __forceinline__ float buoyancy_at(float T, float q, int k, const Cols& c) {
+  const float th0 = c.theta0[k], q0 = c.qv0[k];
+  const float num = th0 * (float)(kReps - 1.0) * (q - q0) + (T - c.d0[k]) * (1.f + (float)kReps * q) * (1.f + q0);
+  return (float)kG * (num / ((1.f + q) * (1.f + q0))) / c.trho0[k];
+}
+
+// ---------------------------------------------------------------------------------------------
+// kernel launchers (stream-ordered; return cudaGetLastError())
+// ---------------------------------------------------------------------------------------------
+struct State {
+  float* T;   // theta - theta_ref
+  float* u;
+  float* v;
+  float* w;   // nz+1 levels
+  float* p;   // pi'
+  float* q;   // qv
+};
+
+struct SlowOut {
+  float* Ru;
+  float* Rv;
+  float* Rw;
+  float* T_next;
+  float* q_next;
+  float* dT;   // optional: d_theta_dt record (adv + sgs)
+  float* dq;   // optional
+};
+
+struct Sgs {
+  const float* u;
+  const float* v;
+  const float* w;
+  const float* T;
+  const float* q;
+};
+
+cudaError_t launch_div_trho(const Dims&, const Phys&, const Cols&, State in, float* div, float* trho, cudaStream_t);
+cudaError_t launch_adv_scalars(const Dims&, const Phys&, const Cols&, State in, const float* div, const float* T0,
+                               const float* q0, Sgs sgs, float dts, SlowOut out, cudaStream_t);
+cudaError_t launch_adv_u(const Dims&, const Phys&, const Cols&, State in, const float* div, const float* sgs_u,
+                         float* Ru, cudaStream_t);
+cudaError_t launch_adv_v(const Dims&, const Phys&, const Cols&, State in, const float* div, const float* sgs_v,
+                         float* Rv, cudaStream_t);
+// mode 0: R_w = adv_w + b8w + sgs_w; mode 1: adv_w only; mode 2: b8w only
+cudaError_t launch_adv_w(const Dims&, const Phys&, const Cols&, State in, const float* div, const float* sgs_w,
+                         float* Rw, int mode, cudaStream_t);
+struct AcousticIn {
+  const float *u, *v, *w, *p;       // sub-step start
+  const float *Ru, *Rv, *Rw;        // slow tendencies
+  const float *trho;                // density potential temperature of the stage state
+  const float *ps;                  // pi' of the stage state (pip_star)
+};
+struct AcousticOut { float *u, *v, *w, *p; };
+cudaError_t launch_acoustic(const Dims&, const Phys&, const Cols&, AcousticIn in, AcousticOut out, float dtau,
+                            cudaStream_t);
+// diagnostics of the acoustic operators on one state
+cudaError_t launch_diag_pgf(const Dims&, const Phys&, const Cols&, const float* p, const float* trho, float* pu,
+                            float* pv, float* pw, cudaStream_t);
+cudaError_t launch_diag_advpi(const Dims&, const Phys&, const Cols&, const float* ps, const float* u,
+                              const float* v, const float* w, float* out, cudaStream_t);
+// Smagorinsky: stage A writes tau11, tau22, tau33, tau12, tau13, tau23, kh (+ optional n2, km)
+struct SmagTau { float *t11, *t22, *t33, *t12, *t13, *t23, *kh, *n2, *km; };
+cudaError_t launch_smag_a(const Dims&, const Phys&, const Cols&, State in, SmagTau out, cudaStream_t);
+struct SgsOut { float *u, *v, *w, *T, *q; };
+cudaError_t launch_smag_b(const Dims&, const Phys&, const Cols&, State in, SmagTau tau, SgsOut out, cudaStream_t);
+
+// layout conversion between the reference's padded [x][y][z] host layout and the device layout
+// kind: 0 scalar, 1 u, 2 v, 3 w
+cudaError_t launch_import_padded(const Dims&, const void* src, int src_f64, int kind, double offset, float* dst,
+                                 cudaStream_t);
+cudaError_t launch_export_padded(const Dims&, const float* src, int kind, double offset, void* dst, int dst_f64,
+                                 cudaStream_t);
+// interior export in reference C order (x slowest, z fastest); u/v with the duplicated face
+cudaError_t launch_export_interior(const Dims&, const float* src, int kind, double offset, double* dst, cudaStream_t);
+
+// FP64 base state
+cudaError_t launch_hydrostatic(int nz, double dz, const double* theta0, const double* qv0, double* pi0,
+                               double* rho0, cudaStream_t);
+cudaError_t launch_build_columns(int nz, double dz, double theta_ref, const double* theta0, const double* qv0,
+                                 const double* pi0, const double* rho0, float* table, cudaStream_t);
+// FP64 budgets: partial sums per block into `partial` (nblocks x 4), then a final pass into out[4]
+int budget_blocks(const Dims&);
+cudaError_t launch_budget(const Dims&, const Phys&, const Cols&, State in, const double* rho0_col,
+                          const double* pi0_col, double theta_ref, double* partial, double* out, cudaStream_t);
+cudaError_t launch_count_nonfinite(const float* a, long long n, unsigned long long* count, cudaStream_t);
+
+}  // namespace lexgb

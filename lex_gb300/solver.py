@@ -1,0 +1,187 @@
+"""Host-side solver object over the C ABI.
+
+``Solver`` owns one device context: the prognostic state stays resident in HBM across
+steps and only crosses to the host on ``download``/``diagnose``.  Arrays exchanged with the
+host use the reference's padded layout (see include/lexgb.h), so the tuples LEX builds in
+setup_lex.py:66-69 can be passed straight through.
+"""
+import ctypes
+import numpy as np
+
+from . import _lib
+from ._lib import check, Config
+
+NGX, NGY, NGZ = 3, 3, 1
+FIELDS = ("theta", "u", "v", "w", "pip", "qv")
+
+
+def padded_shape(nx, ny, nz, field):
+    """Padded reference shape of one prognostic field (setup_lex.py:39-49)."""
+    return (nx + 2 * NGX + (field == "u"), ny + 2 * NGY + (field == "v"), nz + 2 * NGZ + (field == "w"))
+
+
+def interior_shape(nx, ny, nz, field):
+    return (nx + (field == "u"), ny + (field == "v"), nz + (field == "w"))
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Solver:
+    """LEX solver_opt=2 dynamical core on one GPU.
+
+    Parameters mirror namelist_n_constants.py: grid (nx, ny, nz, dx, dy, dz), big-step dt,
+    n_sound acoustic sub-steps per big step, turb_opt (0/1), cor_opt (0/1/2), f_cor.
+    theta_ref is the constant subtracted from theta on the device (0: theta0 at level 1).
+    """
+
+    def __init__(self, nx, ny, nz, dx, dy, dz, dt, n_sound=32, turb_opt=1, cor_opt=0, f_cor=1.0e-4,
+                 theta_ref=0.0):
+        self.lib = _lib.load()
+        cfg = Config()
+        check(self.lib.lexgb_default_config(ctypes.byref(cfg)))
+        cfg.nx, cfg.ny, cfg.nz = nx, ny, nz
+        cfg.dx, cfg.dy, cfg.dz, cfg.dt = dx, dy, dz, dt
+        cfg.n_sound, cfg.turb_opt, cfg.cor_opt = n_sound, turb_opt, cor_opt
+        cfg.f_cor, cfg.theta_ref = f_cor, theta_ref
+        self.cfg = cfg
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.dt = dt
+        self.n_sound = n_sound
+        h = ctypes.c_void_p()
+        check(self.lib.lexgb_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.handle = h
+
+    # -------------------------------------------------------------------------------- lifetime
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.lexgb_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream_handle):
+        """Order work on a CUDA stream given as an integer handle (e.g. torch.cuda.Stream().cuda_stream)."""
+        check(self.lib.lexgb_set_stream(self.handle, ctypes.c_void_p(stream_handle)))
+
+    # -------------------------------------------------------------------------------- base state
+    def _col(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        if a.size != self.nz + 2:
+            raise ValueError("base columns need nz+2 = %d padded levels, got %d" % (self.nz + 2, a.size))
+        return a
+
+    def set_base_columns(self, theta0, qv0, pi0, rho0):
+        cols = [self._col(c) for c in (theta0, qv0, pi0, rho0)]
+        check(self.lib.lexgb_set_base_columns(self.handle, *[_dptr(c) for c in cols]))
+
+    def set_base_state(self, base_state):
+        """From the reference's base_state tuple (rho0_theta0, rho0, theta0, pi0, qv0, surface_t)."""
+        _, rho0, theta0, pi0, qv0, _ = base_state
+        cols = []
+        for name, a in (("theta0", theta0), ("qv0", qv0), ("pi0", pi0), ("rho0", rho0)):
+            a = np.asarray(a, dtype=np.float64)
+            c = a[0, 0, :]
+            if not np.array_equal(a, np.broadcast_to(c, a.shape)):
+                raise ValueError("base state %s is not horizontally uniform" % name)
+            cols.append(c)
+        self.set_base_columns(*cols)
+
+    def integrate_base_state(self, theta0, qv0):
+        """FP64 hydrostatic integration on the GPU; returns padded (pi0, rho0) columns."""
+        t, q = self._col(theta0), self._col(qv0)
+        pi0 = np.empty(self.nz + 2)
+        rho0 = np.empty(self.nz + 2)
+        check(self.lib.lexgb_integrate_base_state(self.handle, _dptr(t), _dptr(q), _dptr(pi0), _dptr(rho0)))
+        return pi0, rho0
+
+    # -------------------------------------------------------------------------------- state transfer
+    def upload(self, state, dtype=None):
+        """Upload the phys_state tuple (theta, u, v, w, pi', qv) in the padded reference layout."""
+        if len(state) != 6:
+            raise ValueError("state must have 6 fields (theta, u, v, w, pip, qv)")
+        if dtype is None:
+            dtype = np.float64 if np.asarray(state[0]).dtype == np.float64 else np.float32
+        arrs = []
+        for name, a in zip(FIELDS, state):
+            a = np.ascontiguousarray(a, dtype=dtype)
+            if a.shape != padded_shape(self.nx, self.ny, self.nz, name):
+                raise ValueError("%s has shape %s, expected %s" % (name, a.shape,
+                                                                    padded_shape(self.nx, self.ny, self.nz, name)))
+            arrs.append(a)
+        ptrs = (ctypes.c_void_p * 6)(*[a.ctypes.data for a in arrs])
+        code = _lib.LEXGB_F64 if dtype == np.float64 else _lib.LEXGB_F32
+        check(self.lib.lexgb_upload_state(self.handle, ptrs, code))
+
+    def upload_ptrs(self, ptrs, f64):
+        """Upload from raw host pointers (e.g. pinned buffers) already in the padded layout."""
+        arr = (ctypes.c_void_p * 6)(*ptrs)
+        check(self.lib.lexgb_upload_state(self.handle, arr, _lib.LEXGB_F64 if f64 else _lib.LEXGB_F32))
+
+    def download_ptrs(self, ptrs, f64):
+        arr = (ctypes.c_void_p * 6)(*ptrs)
+        check(self.lib.lexgb_download_state(self.handle, arr, _lib.LEXGB_F64 if f64 else _lib.LEXGB_F32))
+
+    def download(self, dtype=np.float64):
+        outs = [np.empty(padded_shape(self.nx, self.ny, self.nz, n), dtype=dtype) for n in FIELDS]
+        ptrs = (ctypes.c_void_p * 6)(*[a.ctypes.data for a in outs])
+        code = _lib.LEXGB_F64 if dtype == np.float64 else _lib.LEXGB_F32
+        check(self.lib.lexgb_download_state(self.handle, ptrs, code))
+        return tuple(outs)
+
+    # -------------------------------------------------------------------------------- stepping
+    def step(self, nsteps=1, graph=True):
+        """Advance nsteps RK3 big steps (asynchronous on the context's stream)."""
+        check(self.lib.lexgb_step(self.handle, int(nsteps), 1 if graph else 0))
+
+    def step_record(self):
+        check(self.lib.lexgb_step_record(self.handle))
+
+    def stage(self, s):
+        """After step_record: (padded stage state, interior tendencies) of stage s as FP64 tuples."""
+        f = [np.empty(padded_shape(self.nx, self.ny, self.nz, n)) for n in FIELDS]
+        t = [np.empty(interior_shape(self.nx, self.ny, self.nz, n)) for n in FIELDS]
+        fp = (ctypes.c_void_p * 6)(*[a.ctypes.data for a in f])
+        tp = (ctypes.c_void_p * 6)(*[a.ctypes.data for a in t])
+        check(self.lib.lexgb_download_stage(self.handle, int(s), fp, tp))
+        return tuple(f), tuple(t)
+
+    def synchronize(self):
+        check(self.lib.lexgb_synchronize(self.handle))
+
+    # -------------------------------------------------------------------------------- diagnostics
+    _DIAG_SHAPES = {"adv_u": "u", "adv_v": "v", "adv_w": "w", "buoy_w": "w", "pgf_u": "u", "pgf_v": "v",
+                    "pgf_w": "w", "sgs_u": "u", "sgs_v": "v", "sgs_w": "w"}
+
+    def diagnose(self, name):
+        """One operator of the path evaluated on the current state (FP64, reference C order)."""
+        idx = _lib.DIAGNOSTICS.index(name)
+        out = np.empty(interior_shape(self.nx, self.ny, self.nz, self._DIAG_SHAPES.get(name, "theta")))
+        check(self.lib.lexgb_diagnose(self.handle, idx, _dptr(out)))
+        return out
+
+    def budget(self):
+        out = np.empty(4)
+        check(self.lib.lexgb_budget(self.handle, _dptr(out), 4))
+        return dict(mass=out[0], vapour=out[1], kinetic=out[2], rho_theta=out[3])
+
+    def count_nonfinite(self):
+        n = ctypes.c_longlong()
+        check(self.lib.lexgb_check_finite(self.handle, ctypes.byref(n)))
+        return n.value
+
+    def device_ptrs(self):
+        arr = (ctypes.c_void_p * 6)()
+        check(self.lib.lexgb_state_device_ptrs(self.handle, arr))
+        return [arr[i] for i in range(6)]

@@ -1,0 +1,183 @@
+"""Generate golden vectors by running the reference's own source (LEX) under the NumPy jax stand-in.
+
+Run in a container that has the reference checkout (read-only) at REF_DIR:
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference [--long]
+
+Writes tests/golden/*.npz.  The fixtures pin the oracle (oracle/dycore.py, oracle/ic.py)
+to the reference, and feed the GPU parity tests; nothing at test time reads the reference.
+
+Cases
+  ops_random.npz   random padded state on a 16x12x8 grid (nx != ny): every operator on the
+                   path (divergences, WENO advection of scalars/u/v/w, advection_pi, pressure
+                   gradient, buoyancy, deformation, N^2, Smagorinsky tendencies), one full RK3
+                   step with the three stages' states and tendencies (FP64).
+  bubble_steps.npz the warm-bubble workload on a 16x16x12 grid at 600/600/300 m, dt=3 s:
+                   interior fields after 1, 2, 3 RK3 steps in FP64, and the same from an FP32
+                   run of the reference (to document its own FP32 drift).
+  bubble32_600s.npz the 32x32x32 warm-bubble workload (600/600/300 m, dt = 3 s, Smagorinsky) after
+                   600 s = 200 RK3 steps of the reference in FP64: theta - 300 K, qv - qv0, w and
+                   pi' on the interior, stored as FP32.
+  base_option1.npz the reference's own option-1 base state (setup_lex.py:74-146) columns,
+                   pinning the hydrostatic integration of oracle/ic.py.
+"""
+import os
+import sys
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import jax_standin as js  # noqa: E402
+from oracle.ic import WarmBubble, pad_scalar, pad_u, pad_v  # noqa: E402
+
+MODEL_OPT = (2, False, False, 0, False, False, 1)   # solver 2, Smagorinsky on, all else off
+FIELDS = ("theta", "u", "v", "w", "pip", "qv")
+
+
+def set_namelist(nl, nx, ny, nz, dx, dy, dz, dt, n_sound=32):
+    nl.nx, nl.ny, nl.nz, nl.dx, nl.dy, nl.dz, nl.dt = nx, ny, nz, dx, dy, dz, dt
+    nl.n_sound = n_sound
+    nl.solver_opt, nl.turb_opt = 2, 1
+
+
+def random_state(phys, nx, ny, nz, seed):
+    rng = np.random.default_rng(seed)
+    rnd = lambda shape, s: rng.standard_normal(shape) * s
+    th = pad_scalar(phys[0][3:-3, 3:-3, 1:-1] + rnd((nx, ny, nz), 0.5))
+    ui = rnd((nx, ny, nz), 2.0)
+    u = pad_u(np.concatenate([ui, ui[:1]], 0))
+    vi = rnd((nx, ny, nz), 2.0)
+    v = pad_v(np.concatenate([vi, vi[:, :1]], 1))
+    wi = rnd((nx, ny, nz + 1), 1.0)
+    wi[:, :, 0] = 0.0
+    wi[:, :, -1] = 0.0
+    w = pad_scalar(wi)
+    pip = pad_scalar(rnd((nx, ny, nz), 1e-4))
+    qv = pad_scalar(phys[5][3:-3, 3:-3, 1:-1] * (1.0 + rnd((nx, ny, nz), 0.05)))
+    return (th, u, v, w, pip, qv)
+
+
+def columns(base):
+    rho0_theta0, rho0, theta0, pi0, qv0, _ = base
+    return dict(col_theta0=theta0[0, 0], col_qv0=qv0[0, 0], col_pi0=pi0[0, 0], col_rho0=rho0[0, 0])
+
+
+def case_ops(R, out):
+    nl = R.nl
+    nx, ny, nz, dx, dy, dz, dt = 16, 12, 8, 600.0, 500.0, 300.0, 3.0
+    set_namelist(nl, nx, ny, nz, dx, dy, dz, dt)
+    phys, base, grids = WarmBubble(nx, ny, nz, dx, dy, dz).build()
+    state = random_state(phys, nx, ny, nz, seed=11)
+    js.set_dtype(np.float64)
+    c = js._cast_tree
+    state, base, grids = c(state), c(base), c(grids)
+    th, u, v, w, pip, qv = state
+    _, rho0, theta0, pi0, qv0, _ = base
+    x3d, y3d, z3d, x3d4u, y3d4v, z3d4w, cc1, cc2, _, _ = grids
+    z2 = np.zeros((nx, ny))
+    d = dict(nx=nx, ny=ny, nz=nz, dx=dx, dy=dy, dz=dz, dt=dt, n_sound=32, **columns(base))
+    for k, a in zip(FIELDS, state):
+        d["in_" + k] = np.asarray(a)
+    div = R.adv.get_divergence(rho0, u, v, w, x3d4u, y3d4v, z3d4w)
+    d["mass_div"] = div
+    d["vel_div"] = R.adv.get_divergence2(u, v, w, x3d4u, y3d4v, z3d4w)
+    d["adv_theta"] = R.adv.advection_scalar(rho0, th, u, v, w, 1e-17, div, z2, x3d4u, y3d4v, z3d4w)
+    d["adv_qv"] = R.adv.advection_scalar(rho0, qv, u, v, w, 1e-18, div, z2, x3d4u, y3d4v, z3d4w)
+    d["adv_u"], d["adv_v"], d["adv_w"] = R.one.prep_momentum_eqn(rho0, u, v, w, div, z2, z2, x3d, y3d, z3d,
+                                                                  x3d4u, y3d4v, z3d4w)
+    d["adv_pi"] = R.adv.advection_pi(rho0, pi0, pip, u, v, w, x3d, y3d, z3d, cc1, cc2)
+    trho = th * (1.0 + nl.reps * qv) / (1.0 + qv)
+    d["theta_rho"] = trho
+    d["pgf_u"], d["pgf_v"], d["pgf_w"] = R.pres_grad.pressure_gradient_force(pi0, pip, trho, x3d, y3d, z3d)
+    d["buoy"], d["buoy_w"] = R.pres_eqn.calculate_buoyancy(theta0, th, qv0, qv)
+    s11, s22, s33, s12, s13, s23, s2 = R.turb.compute_deformation(rho0, u, v, w, x3d, y3d, z3d, x3d4u, y3d4v, z3d4w)
+    for k, a in zip(("s11", "s22", "s33", "s12", "s13", "s23", "s2"), (s11, s22, s33, s12, s13, s23, s2)):
+        d["def_" + k] = a
+    n2 = R.turb.compute_nm(th, pi0, qv, z3d)
+    d["n2"] = n2
+    km, kh = R.turb.compute_k(s2, n2, x3d4u, y3d4v, z3d4w)
+    d["km"], d["kh"] = km, kh
+    sg = R.turb.compute_smag(rho0, km, kh, s11, s22, s33, s12, s13, s23, th, qv, x3d, y3d, z3d, x3d4u, y3d4v, z3d4w)
+    for k, a in zip(("u", "v", "w", "theta", "qv"), sg):
+        d["sgs_" + k] = a
+    # the three WS-RK3 stages of one big step (one_sprint_functions.py:17-21)
+    xi1, t1, sfc, heat, sgs_t = R.one.rk_sub_step0(state, state, base, grids, MODEL_OPT, nl.dt / 3.0)
+    xi2, t2 = R.one.rk_sub_step1(state, xi1, base, grids, heat, sfc, sgs_t, MODEL_OPT, nl.dt / 2.0)
+    xi3, t3 = R.one.rk_sub_step2(state, xi2, base, grids, heat, sfc, sgs_t, MODEL_OPT, nl.dt)
+    tnames = ("dtheta", "dpip", "du", "dv", "dw", "dqv")
+    for s, (xi, tt) in enumerate(((xi1, t1), (xi2, t2), (xi3, t3))):
+        for k, a in zip(FIELDS, xi):
+            d["stage%d_%s" % (s, k)] = a
+        for k, a in zip(tnames, tt):
+            d["stage%d_%s" % (s, k)] = a
+    step, _ = R.sp.ws_rk3_big_step(state, base, grids, MODEL_OPT)
+    for k, a in zip(FIELDS, step):
+        d["step_" + k] = a
+    d = {k: np.asarray(v) for k, v in d.items()}
+    np.savez_compressed(out, **d)
+
+
+def case_bubble(R, out, nsteps=3):
+    nl = R.nl
+    nx, ny, nz, dx, dy, dz, dt = 16, 16, 12, 600.0, 600.0, 300.0, 3.0
+    set_namelist(nl, nx, ny, nz, dx, dy, dz, dt)
+    wb = WarmBubble(nx, ny, nz, dx, dy, dz)
+    phys, base, grids = wb.build()
+    d = dict(nx=nx, ny=ny, nz=nz, dx=dx, dy=dy, dz=dz, dt=dt, n_sound=32, seed=wb.seed, **columns(base))
+    for k, a in zip(FIELDS, phys):
+        d["in_" + k] = a
+    for tag, dtype in (("f64", np.float64), ("f32", np.float32)):
+        js.set_dtype(dtype)
+        st = phys
+        for n in range(nsteps):
+            st, _ = R.sp.ws_rk3_big_step(st, base, grids, MODEL_OPT)
+            for k, a in zip(FIELDS, st):
+                d["%s_step%d_%s" % (tag, n + 1, k)] = np.asarray(a, dtype=dtype)
+    np.savez_compressed(out, **{k: np.asarray(v) for k, v in d.items()})
+
+
+def case_bubble_600s(R, out, nsteps=200):
+    nl = R.nl
+    nx, ny, nz, dx, dy, dz, dt = 32, 32, 32, 600.0, 600.0, 300.0, 3.0
+    set_namelist(nl, nx, ny, nz, dx, dy, dz, dt)
+    wb = WarmBubble(nx, ny, nz, dx, dy, dz)
+    phys, base, grids = wb.build()
+    js.set_dtype(np.float64)
+    st = phys
+    for _ in range(nsteps):
+        st, _ = R.sp.ws_rk3_big_step(st, base, grids, MODEL_OPT)
+    th, u, v, w, pip, qv = (np.asarray(a) for a in st)
+    qv0 = base[4]
+    inner = (slice(3, -3), slice(3, -3), slice(1, -1))
+    np.savez_compressed(out, nx=nx, ny=ny, nz=nz, dx=dx, dy=dy, dz=dz, dt=dt, n_sound=32, seed=wb.seed,
+                        nsteps=nsteps, theta_p=(th[inner] - 300.0).astype(np.float32),
+                        qv_p=(qv[inner] - qv0[inner]).astype(np.float32),
+                        w=w[3:-3, 3:-3, 1:-1].astype(np.float32), pip=pip[inner].astype(np.float32))
+
+
+def case_base(R, out):
+    nl = R.nl
+    nx, ny, nz, dz = 4, 4, 40, 100.0
+    set_namelist(nl, nx, ny, nz, 100.0, 100.0, dz, 1.0)
+    js.set_dtype(np.float64)
+    phys, base, grids, _ = R.setl.setup_grid_n_ic(1)
+    rho0_theta0, rho0, theta0, pi0, qv0, _ = base
+    np.savez_compressed(out, nz=nz, dz=dz, rho0=np.asarray(rho0)[0, 0], theta0=np.asarray(theta0)[0, 0],
+                        pi0=np.asarray(pi0)[0, 0], qv0=np.asarray(qv0)[0, 0],
+                        rho0_theta0=np.asarray(rho0_theta0)[0, 0])
+
+
+def main(ref_dir):
+    R = js.load_reference(ref_dir)
+    case_ops(R, os.path.join(HERE, "ops_random.npz"))
+    case_bubble(R, os.path.join(HERE, "bubble_steps.npz"))
+    case_base(R, os.path.join(HERE, "base_option1.npz"))
+    if "--long" in sys.argv:
+        case_bubble_600s(R, os.path.join(HERE, "bubble32_600s.npz"))
+
+
+if __name__ == "__main__":
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    main(args[0] if args else "/root/reference")
