@@ -141,6 +141,25 @@ int lexgb_synchronize(lexgb_ctx *ctx);
  * theta stored minus theta_ref, u/v periodic without the duplicated face, w with nz+1 levels). */
 int lexgb_state_device_ptrs(lexgb_ctx *ctx, void *ptrs[6]);
 
+/* Kernels of one big step, for timing: the number of kernel nodes in the captured CUDA graph
+ * of one big step (captures it if needed). */
+int lexgb_step_kernel_count(lexgb_ctx *ctx, int *n_kernels);
+
+/* Time `reps` back-to-back launches of one kernel of the step on the context's stream with CUDA
+ * events (state untouched: outputs go to scratch).  *ms_per_launch = average launch duration. */
+enum {
+    LEXGB_KERNEL_ACOUSTIC = 0,  /* one acoustic sub-step */
+    LEXGB_KERNEL_DIV_TRHO,      /* mass divergence + theta_rho */
+    LEXGB_KERNEL_ADV_SCALARS,   /* theta and qv advection + Euler update */
+    LEXGB_KERNEL_ADV_U,
+    LEXGB_KERNEL_ADV_V,
+    LEXGB_KERNEL_ADV_W,
+    LEXGB_KERNEL_SMAG_A,
+    LEXGB_KERNEL_SMAG_B,
+    LEXGB_KERNEL_COUNT
+};
+int lexgb_time_kernel(lexgb_ctx *ctx, int which, int reps, float *ms_per_launch);
+
 /* Message of the last failure on this thread; returns the untruncated length. */
 int lexgb_last_error(char *buf, size_t len);
 

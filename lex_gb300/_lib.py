@@ -16,6 +16,8 @@ DIAGNOSTICS = ["mass_div", "adv_theta", "adv_qv", "adv_u", "adv_v", "adv_w", "bu
                "pgf_u", "pgf_v", "pgf_w", "adv_pi", "sgs_u", "sgs_v", "sgs_w", "sgs_theta", "sgs_qv",
                "n2", "km"]
 
+KERNELS = ["acoustic", "div_trho", "adv_scalars", "adv_u", "adv_v", "adv_w", "smag_a", "smag_b"]
+
 # every entry point include/lexgb.h declares: name -> (restype, argtypes)
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -47,6 +49,8 @@ SIGNATURES = {
     "lexgb_check_finite": (_I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     "lexgb_synchronize": (_I, [_P]),
     "lexgb_state_device_ptrs": (_I, [_P, ctypes.POINTER(_P)]),
+    "lexgb_step_kernel_count": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "lexgb_time_kernel": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_float)]),
     "lexgb_last_error": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
 }
 

@@ -625,6 +625,81 @@ int lexgb_state_device_ptrs(lexgb_ctx* c, void* ptrs[6]) {
   return LEXGB_OK;
 }
 
+int lexgb_step_kernel_count(lexgb_ctx* c, int* n_kernels) {
+  CKS(check_ready(c));
+  if (!n_kernels) return fail(LEXGB_ERR_ARG, "null output");
+  if (!c->gexec) CKS(lexgb_step(c, 0, 1));
+  size_t n = 0;
+  CK(cudaGraphGetNodes(c->graph, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  CK(cudaGraphGetNodes(c->graph, nodes.data(), &n));
+  int k = 0;
+  for (size_t i = 0; i < n; ++i) {
+    cudaGraphNodeType t;
+    CK(cudaGraphNodeGetType(nodes[i], &t));
+    k += t == cudaGraphNodeTypeKernel;
+  }
+  *n_kernels = k;
+  return LEXGB_OK;
+}
+
+int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
+  CKS(check_ready(c));
+  if (!ms_per_launch || reps < 1) return fail(LEXGB_ERR_ARG, "need reps >= 1 and an output");
+  if (which < 0 || which >= LEXGB_KERNEL_COUNT) return fail(LEXGB_ERR_ARG, "unknown kernel");
+  const Dims& d = c->d;
+  const StagePlan p = plan_of(c->cfg);
+  const State& x = c->A;
+  // inputs that the timed kernels read: slow tendencies of the current state
+  CK(launch_div_trho(d, c->ph, c->cols, x, c->div, c->trho, c->stream));
+  SmagTau t{c->tau[0], c->tau[1], c->tau[2], c->tau[3], c->tau[4], c->tau[5], c->tau[6], nullptr, nullptr};
+  const Sgs sg{c->sgs[0], c->sgs[1], c->sgs[2], c->sgs[3], c->sgs[4]};
+  SlowOut so{nullptr, nullptr, nullptr, c->B.T, c->B.q, nullptr, nullptr};
+  const AcousticOut X{c->Xu, c->Xv, c->Xw, c->Xp}, Y{c->Yu, c->Yv, c->Yw, c->Yp};
+  AcousticIn in{x.u, x.v, x.w, x.p, c->Ru, c->Rv, c->Rw, c->trho, x.p};
+  auto launch = [&](int r) -> cudaError_t {
+    switch (which) {
+      case LEXGB_KERNEL_ACOUSTIC: {
+        const AcousticOut o = (r & 1) ? Y : X;
+        cudaError_t e = launch_acoustic(d, c->ph, c->cols, in, o, (float)p.dtau[2], c->stream);
+        in.u = o.u; in.v = o.v; in.w = o.w; in.p = o.p;
+        return e;
+      }
+      case LEXGB_KERNEL_DIV_TRHO: return launch_div_trho(d, c->ph, c->cols, x, c->div, c->trho, c->stream);
+      case LEXGB_KERNEL_ADV_SCALARS:
+        return launch_adv_scalars(d, c->ph, c->cols, x, c->div, x.T, x.q, sg, (float)p.dts[2], so, c->stream);
+      case LEXGB_KERNEL_ADV_U: return launch_adv_u(d, c->ph, c->cols, x, c->div, sg.u, c->Ru, c->stream);
+      case LEXGB_KERNEL_ADV_V: return launch_adv_v(d, c->ph, c->cols, x, c->div, sg.v, c->Rv, c->stream);
+      case LEXGB_KERNEL_ADV_W: return launch_adv_w(d, c->ph, c->cols, x, c->div, sg.w, c->Rw, 0, c->stream);
+      case LEXGB_KERNEL_SMAG_A: return launch_smag_a(d, c->ph, c->cols, x, t, c->stream);
+      default: {
+        SgsOut o{c->sgs[0], c->sgs[1], c->sgs[2], c->sgs[3], c->sgs[4]};
+        return launch_smag_b(d, c->ph, c->cols, x, t, o, c->stream);
+      }
+    }
+  };
+  // populate every input the timed kernel reads, then warm up once
+  CK(launch_smag_a(d, c->ph, c->cols, x, t, c->stream));
+  CK(launch_adv_u(d, c->ph, c->cols, x, c->div, nullptr, c->Ru, c->stream));
+  CK(launch_adv_v(d, c->ph, c->cols, x, c->div, nullptr, c->Rv, c->stream));
+  CK(launch_adv_w(d, c->ph, c->cols, x, c->div, nullptr, c->Rw, 0, c->stream));
+  CK(launch(0));
+  in = AcousticIn{x.u, x.v, x.w, x.p, c->Ru, c->Rv, c->Rw, c->trho, x.p};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, c->stream));
+  for (int r = 0; r < reps; ++r) CK(launch(r));
+  CK(cudaEventRecord(e1, c->stream));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms_per_launch = ms / reps;
+  return LEXGB_OK;
+}
+
 int lexgb_last_error(char* buf, size_t len) {
   if (buf && len) {
     const size_t n = g_last_error.size() < len - 1 ? g_last_error.size() : len - 1;

@@ -93,6 +93,89 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_acoustic(Dims d, Phys ph, Cols c
   if (k == d.nz - 1) o.w[d.at(i, j, d.nz)] = 0.f;
 }
 
+// Vectorised sub-step: each thread owns 4 consecutive x points of one (j, k) row and moves
+// every field with 128-bit loads/stores (needs nx % 4 == 0).  Same arithmetic as k_acoustic.
+__device__ __forceinline__ float4 ld4(const float* __restrict__ p, int idx) {
+  return __ldg(reinterpret_cast<const float4*>(p + idx));
+}
+__device__ __forceinline__ float comp(const float4& v, int l) { return l == 0 ? v.x : (l == 1 ? v.y : (l == 2 ? v.z : v.w)); }
+
+__global__ void __launch_bounds__(256) k_acoustic4(Dims d, Phys ph, Cols c, AcousticIn a, AcousticOut o,
+                                                   float dtau) {
+  const int nq = d.nx >> 2;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (q >= nq || j >= d.ny) return;
+  const int nx = d.nx, nz = d.nz;
+  const int i0 = q << 2;
+  const int iw = wrap(i0 - 1, nx), ie = wrap(i0 + 4, nx);
+  const int jm = wrap(j - 1, d.ny), jp = wrap(j + 1, d.ny);
+  const int r0 = (k * d.ny + j) * nx;
+  const int rs = (k * d.ny + jm) * nx, rn = (k * d.ny + jp) * nx;
+  const int rb = r0 - d.plane(), rt = r0 + d.plane();
+  const bool has_b = k > 0, has_t = k + 1 < nz;
+  // centre row
+  const float4 P = ld4(a.p, r0 + i0), TR = ld4(a.trho, r0 + i0), U = ld4(a.u, r0 + i0), RU = ld4(a.Ru, r0 + i0);
+  const float pW = __ldg(a.p + r0 + iw), pE = __ldg(a.p + r0 + ie);
+  const float tW = __ldg(a.trho + r0 + iw), tE = __ldg(a.trho + r0 + ie);
+  const float uE = __ldg(a.u + r0 + ie), ruE = __ldg(a.Ru + r0 + ie);
+  // south / north rows
+  const float4 V = ld4(a.v, r0 + i0), RV = ld4(a.Rv, r0 + i0);
+  const float4 PS = ld4(a.p, rs + i0), TS = ld4(a.trho, rs + i0);
+  const float4 VN = ld4(a.v, rn + i0), RVN = ld4(a.Rv, rn + i0);
+  const float4 PN = ld4(a.p, rn + i0), TN = ld4(a.trho, rn + i0);
+  // bottom / top levels
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 W = has_b ? ld4(a.w, r0 + i0) : z4, RW = has_b ? ld4(a.Rw, r0 + i0) : z4;
+  const float4 PB = has_b ? ld4(a.p, rb + i0) : z4, TB = has_b ? ld4(a.trho, rb + i0) : z4;
+  const float4 WT = has_t ? ld4(a.w, rt + i0) : z4, RWT = has_t ? ld4(a.Rw, rt + i0) : z4;
+  const float4 PT = has_t ? ld4(a.p, rt + i0) : z4, TT = has_t ? ld4(a.trho, rt + i0) : z4;
+  // pi'_s for advection_pi
+  const float4 S0 = ld4(a.ps, r0 + i0), SS = ld4(a.ps, rs + i0), SN = ld4(a.ps, rn + i0);
+  const float4 SB = has_b ? ld4(a.ps, rb + i0) : z4, ST = has_t ? ld4(a.ps, rt + i0) : z4;
+  const float sW = __ldg(a.ps + r0 + iw), sE = __ldg(a.ps + r0 + ie);
+
+  float un[5];
+  {
+    const float pc[6] = {pW, P.x, P.y, P.z, P.w, pE};
+    const float tc[6] = {tW, TR.x, TR.y, TR.z, TR.w, tE};
+    const float uc[5] = {U.x, U.y, U.z, U.w, uE};
+    const float rc[5] = {RU.x, RU.y, RU.z, RU.w, ruE};
+#pragma unroll
+    for (int l = 0; l < 5; ++l) un[l] = uc[l] + (pgf(tc[l + 1], tc[l], pc[l + 1], pc[l], ph.rdx) + rc[l]) * dtau;
+  }
+  const float sc[6] = {sW, S0.x, S0.y, S0.z, S0.w, sE};
+  const float rho = c.rho[k], rfb = c.rho_face[k], rft = c.rho_face[k + 1];
+  const float dzb = c.dpi0dz[k], dzt = c.dpi0dz[k + 1], pi0 = c.pi0[k];
+  float outp[4], outv[4], outw[4];
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    const float p0 = comp(P, l), t0 = comp(TR, l);
+    const float vs = comp(V, l) + (pgf(t0, comp(TS, l), p0, comp(PS, l), ph.rdy) + comp(RV, l)) * dtau;
+    const float vn = comp(VN, l) + (pgf(comp(TN, l), t0, comp(PN, l), p0, ph.rdy) + comp(RVN, l)) * dtau;
+    const float wb = has_b ? comp(W, l) + (pgf(t0, comp(TB, l), p0, comp(PB, l), ph.rdz) + comp(RW, l)) * dtau : 0.f;
+    const float wt = has_t ? comp(WT, l) + (pgf(comp(TT, l), t0, comp(PT, l), p0, ph.rdz) + comp(RWT, l)) * dtau : 0.f;
+    const float div = (un[l + 1] - un[l]) * ph.rdx + (vn - vs) * ph.rdy + (wt - wb) * ph.rdz;
+    const float s0 = sc[l + 1];
+    const float gxw = (s0 - sc[l]) * ph.rdx, gxe = (sc[l + 2] - s0) * ph.rdx;
+    const float gys = (s0 - comp(SS, l)) * ph.rdy, gyn = (comp(SN, l) - s0) * ph.rdy;
+    const float wzb = has_b ? wb * (dzb + (s0 - comp(SB, l)) * ph.rdz) : 0.f;
+    const float wzt = has_t ? wt * (dzt + (comp(ST, l) - s0) * ph.rdz) : 0.f;
+    const float ap = -(0.5f * (un[l + 1] * gxe + un[l] * gxw) + 0.5f * (vn * gyn + vs * gys) +
+                       (0.5f * wzb * rfb + 0.5f * wzt * rft) / rho);
+    const float dpdt = -kRdCv * ((pi0 + s0) * div) + ap;
+    outp[l] = p0 + (kDivDamp * dpdt) * dtau;
+    outv[l] = vs;
+    outw[l] = wb;
+  }
+  *reinterpret_cast<float4*>(o.p + r0 + i0) = make_float4(outp[0], outp[1], outp[2], outp[3]);
+  *reinterpret_cast<float4*>(o.u + r0 + i0) = make_float4(un[0], un[1], un[2], un[3]);
+  *reinterpret_cast<float4*>(o.v + r0 + i0) = make_float4(outv[0], outv[1], outv[2], outv[3]);
+  *reinterpret_cast<float4*>(o.w + r0 + i0) = make_float4(outw[0], outw[1], outw[2], outw[3]);
+  if (k == nz - 1) *reinterpret_cast<float4*>(o.w + rt + i0) = z4;
+}
+
 __global__ void k_diag_pgf(Dims d, Phys ph, Cols c, const float* __restrict__ p, const float* __restrict__ trho,
                            float* pu, float* pv, float* pw) {
   const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y, f = blockIdx.z * BZ + threadIdx.z;
@@ -126,6 +209,13 @@ __global__ void k_diag_advpi(Dims d, Phys ph, Cols c, const float* __restrict__ 
 
 cudaError_t launch_acoustic(const Dims& d, const Phys& ph, const Cols& c, AcousticIn in, AcousticOut out, float dtau,
                             cudaStream_t st) {
+  if (d.nx % 4 == 0) {
+    const int nq = d.nx / 4;
+    dim3 b(16, 16, 1);
+    dim3 g((nq + b.x - 1) / b.x, (d.ny + b.y - 1) / b.y, d.nz);
+    k_acoustic4<<<g, b, 0, st>>>(d, ph, c, in, out, dtau);
+    return cudaGetLastError();
+  }
   dim3 g((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, (d.nz + BZ - 1) / BZ);
   k_acoustic<<<g, dim3(BX, BY, BZ), 0, st>>>(d, ph, c, in, out, dtau);
   return cudaGetLastError();

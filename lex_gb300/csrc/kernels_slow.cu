@@ -53,19 +53,19 @@ __device__ __forceinline__ float scalar_tendency(const Dims& d, const Phys& ph, 
   // x faces i (west) and i+1 (east)
   const float mw = r * LD(s.u, d.at(i, j, k));
   const float me = r * LD(s.u, d.at(wrap(i + 1, nx), j, k));
-  const float fw = upwind(mw, weno5(x[0], x[1], x[2], x[3], x[4], eps), weno5(x[5], x[4], x[3], x[2], x[1], eps));
-  const float fe = upwind(me, weno5(x[1], x[2], x[3], x[4], x[5], eps), weno5(x[6], x[5], x[4], x[3], x[2], eps));
+  const float fw = weno_flux(mw, x[0], x[1], x[2], x[3], x[4], x[5], eps);
+  const float fe = weno_flux(me, x[1], x[2], x[3], x[4], x[5], x[6], eps);
   const float ms = r * LD(s.v, d.at(i, j, k));
   const float mn = r * LD(s.v, d.at(i, wrap(j + 1, ny), k));
-  const float fs = upwind(ms, weno5(y[0], y[1], y[2], y[3], y[4], eps), weno5(y[5], y[4], y[3], y[2], y[1], eps));
-  const float fn = upwind(mn, weno5(y[1], y[2], y[3], y[4], y[5], eps), weno5(y[6], y[5], y[4], y[3], y[2], eps));
+  const float fs = weno_flux(ms, y[0], y[1], y[2], y[3], y[4], y[5], eps);
+  const float fn = weno_flux(mn, y[1], y[2], y[3], y[4], y[5], y[6], eps);
   auto colv = [&](int kk) { return LD(f, d.at(i, j, kk)); };
   float fz[2];
 #pragma unroll
   for (int o = 0; o < 2; ++o) {
     const int fk = k + o;
     const float m = c.rho_face[fk] * LD(s.w, d.at(i, j, fk));
-    fz[o] = (fk == 0) ? 0.f : upwind(m, vrecon(colv, fk, nz, true, eps), vrecon(colv, fk, nz, false, eps));
+    fz[o] = (fk == 0) ? 0.f : vflux(m, colv, fk, nz, eps);
   }
   const float conv = -((fe - fw) * ph.rdx + (fn - fs) * ph.rdy + (fz[1] - fz[0]) * ph.rdz);
   const int id = d.at(i, j, k);
@@ -114,16 +114,14 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_adv_u(Dims d, Phys ph, Cols c, S
     y[o] = LD(s.u, d.at(i, wrap(j - 3 + o, ny), k));
   }
   // x flux at the cells west (i-1) and east (i) of u(i)
-  const float fw = upwind(0.5f * (x[2] + x[3]) * r, weno5(x[0], x[1], x[2], x[3], x[4], eps),
-                          weno5(x[5], x[4], x[3], x[2], x[1], eps));
-  const float fe = upwind(0.5f * (x[3] + x[4]) * r, weno5(x[1], x[2], x[3], x[4], x[5], eps),
-                          weno5(x[6], x[5], x[4], x[3], x[2], eps));
+  const float fw = weno_flux(0.5f * (x[2] + x[3]) * r, x[0], x[1], x[2], x[3], x[4], x[5], eps);
+  const float fe = weno_flux(0.5f * (x[3] + x[4]) * r, x[1], x[2], x[3], x[4], x[5], x[6], eps);
   // y flux at the corners south (face j) and north (face j+1) of u(i, j)
   const int jp = wrap(j + 1, ny);
   const float ms = 0.5f * (r * LD(s.v, d.at(im, j, k)) + r * LD(s.v, d.at(i, j, k)));
   const float mn = 0.5f * (r * LD(s.v, d.at(im, jp, k)) + r * LD(s.v, d.at(i, jp, k)));
-  const float fs = upwind(ms, weno5(y[0], y[1], y[2], y[3], y[4], eps), weno5(y[5], y[4], y[3], y[2], y[1], eps));
-  const float fn = upwind(mn, weno5(y[1], y[2], y[3], y[4], y[5], eps), weno5(y[6], y[5], y[4], y[3], y[2], eps));
+  const float fs = weno_flux(ms, y[0], y[1], y[2], y[3], y[4], y[5], eps);
+  const float fn = weno_flux(mn, y[1], y[2], y[3], y[4], y[5], y[6], eps);
   auto colv = [&](int kk) { return LD(s.u, d.at(i, j, kk)); };
   float fz[2];
 #pragma unroll
@@ -131,7 +129,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_adv_u(Dims d, Phys ph, Cols c, S
     const int fk = k + o;
     const float rf = c.rho_face[fk];
     const float m = 0.5f * (rf * LD(s.w, d.at(im, j, fk)) + rf * LD(s.w, d.at(i, j, fk)));
-    fz[o] = (fk == 0) ? 0.f : upwind(m, vrecon(colv, fk, nz, true, eps), vrecon(colv, fk, nz, false, eps));
+    fz[o] = (fk == 0) ? 0.f : vflux(m, colv, fk, nz, eps);
   }
   const float conv = -((fe - fw) * ph.rdx + (fn - fs) * ph.rdy + (fz[1] - fz[0]) * ph.rdz);
   const float d8u = 0.5f * (LD(div, d.at(im, j, k)) + LD(div, d.at(i, j, k)));
@@ -163,13 +161,11 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_adv_v(Dims d, Phys ph, Cols c, S
   const int ip = wrap(i + 1, nx);
   const float mw = 0.5f * (r * LD(s.u, d.at(i, jm, k)) + r * LD(s.u, d.at(i, j, k)));
   const float me = 0.5f * (r * LD(s.u, d.at(ip, jm, k)) + r * LD(s.u, d.at(ip, j, k)));
-  const float fw = upwind(mw, weno5(x[0], x[1], x[2], x[3], x[4], eps), weno5(x[5], x[4], x[3], x[2], x[1], eps));
-  const float fe = upwind(me, weno5(x[1], x[2], x[3], x[4], x[5], eps), weno5(x[6], x[5], x[4], x[3], x[2], eps));
+  const float fw = weno_flux(mw, x[0], x[1], x[2], x[3], x[4], x[5], eps);
+  const float fe = weno_flux(me, x[1], x[2], x[3], x[4], x[5], x[6], eps);
   // y flux at the cells south (j-1) and north (j) of v(j)
-  const float fs = upwind(0.5f * (y[2] + y[3]) * r, weno5(y[0], y[1], y[2], y[3], y[4], eps),
-                          weno5(y[5], y[4], y[3], y[2], y[1], eps));
-  const float fn = upwind(0.5f * (y[3] + y[4]) * r, weno5(y[1], y[2], y[3], y[4], y[5], eps),
-                          weno5(y[6], y[5], y[4], y[3], y[2], eps));
+  const float fs = weno_flux(0.5f * (y[2] + y[3]) * r, y[0], y[1], y[2], y[3], y[4], y[5], eps);
+  const float fn = weno_flux(0.5f * (y[3] + y[4]) * r, y[1], y[2], y[3], y[4], y[5], y[6], eps);
   auto colv = [&](int kk) { return LD(s.v, d.at(i, j, kk)); };
   float fz[2];
 #pragma unroll
@@ -177,7 +173,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_adv_v(Dims d, Phys ph, Cols c, S
     const int fk = k + o;
     const float rf = c.rho_face[fk];
     const float m = 0.5f * (rf * LD(s.w, d.at(i, jm, fk)) + rf * LD(s.w, d.at(i, j, fk)));
-    fz[o] = (fk == 0) ? 0.f : upwind(m, vrecon(colv, fk, nz, true, eps), vrecon(colv, fk, nz, false, eps));
+    fz[o] = (fk == 0) ? 0.f : vflux(m, colv, fk, nz, eps);
   }
   const float conv = -((fe - fw) * ph.rdx + (fn - fs) * ph.rdy + (fz[1] - fz[0]) * ph.rdz);
   const float d8v = 0.5f * (LD(div, d.at(i, jm, k)) + LD(div, d.at(i, j, k)));
@@ -212,12 +208,12 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_adv_w(Dims d, Phys ph, Cols c, S
     // x flux at u points i and i+1 on face f
     const float mw = 0.5f * (rl * LD(s.u, d.at(i, j, f - 1)) + ru * LD(s.u, d.at(i, j, f)));
     const float me = 0.5f * (rl * LD(s.u, d.at(ip, j, f - 1)) + ru * LD(s.u, d.at(ip, j, f)));
-    const float fw = upwind(mw, weno5(x[0], x[1], x[2], x[3], x[4], eps), weno5(x[5], x[4], x[3], x[2], x[1], eps));
-    const float fe = upwind(me, weno5(x[1], x[2], x[3], x[4], x[5], eps), weno5(x[6], x[5], x[4], x[3], x[2], eps));
+    const float fw = weno_flux(mw, x[0], x[1], x[2], x[3], x[4], x[5], eps);
+    const float fe = weno_flux(me, x[1], x[2], x[3], x[4], x[5], x[6], eps);
     const float ms = 0.5f * (rl * LD(s.v, d.at(i, j, f - 1)) + ru * LD(s.v, d.at(i, j, f)));
     const float mn = 0.5f * (rl * LD(s.v, d.at(i, jp, f - 1)) + ru * LD(s.v, d.at(i, jp, f)));
-    const float fs = upwind(ms, weno5(y[0], y[1], y[2], y[3], y[4], eps), weno5(y[5], y[4], y[3], y[2], y[1], eps));
-    const float fn = upwind(mn, weno5(y[1], y[2], y[3], y[4], y[5], eps), weno5(y[6], y[5], y[4], y[3], y[2], eps));
+    const float fs = weno_flux(ms, y[0], y[1], y[2], y[3], y[4], y[5], eps);
+    const float fn = weno_flux(mn, y[1], y[2], y[3], y[4], y[5], y[6], eps);
     // z flux at the cells below (f-1) and above (f) the face, w column has nz+1 entries
     auto colw = [&](int kk) { return LD(s.w, d.at(i, j, kk)); };
     float fz[2];
@@ -225,7 +221,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_adv_w(Dims d, Phys ph, Cols c, S
     for (int o = 0; o < 2; ++o) {
       const int cc = f - 1 + o;
       const float m = 0.5f * (colw(cc) + colw(cc + 1)) * c.rho[cc];
-      fz[o] = upwind(m, vrecon(colw, cc + 1, nz + 1, true, eps), vrecon(colw, cc + 1, nz + 1, false, eps));
+      fz[o] = vflux(m, colw, cc + 1, nz + 1, eps);
     }
     const float conv = -((fe - fw) * ph.rdx + (fn - fs) * ph.rdy + (fz[1] - fz[0]) * ph.rdz);
     const float d8w = 0.5f * (LD(div, d.at(i, j, f - 1)) + LD(div, d.at(i, j, f)));

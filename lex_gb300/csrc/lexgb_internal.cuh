@@ -136,6 +136,26 @@ __device__ __forceinline__ float vrecon(const F& s, int f, int n, bool up, float
 // jax.lax.select(m >= 0, m*pos, m*neg): ties take the positive branch.
 __device__ __forceinline__ float upwind(float m, float pos, float neg) { return m >= 0.f ? m * pos : m * neg; }
 
+// m * (upwind WENO5 value) at the face between s[-1] and s[0], given s[-3..2]: the stencil is
+// selected by the sign of the mass flux first, so only one reconstruction is evaluated
+// (the reference evaluates both and selects, advection.py:505).
+__device__ __forceinline__ float weno_flux(float m, float sm3, float sm2, float sm1, float s0, float sp1, float sp2,
+                                           float eps) {
+  const bool p = m >= 0.f;
+  return m * weno5(p ? sm3 : sp2, p ? sm2 : sp1, p ? sm1 : s0, p ? s0 : sm1, p ? sp1 : sm2, eps);
+}
+
+// m * (upwind vertical face value) at face f of an n-entry column (see vrecon); zero at the ends.
+template <class F>
+__device__ __forceinline__ float vflux(float m, const F& s, int f, int n, float eps) {
+  if (f <= 0 || f >= n) return 0.f;
+  const bool up = m >= 0.f;
+  if (f >= 3 && f <= n - 3)
+    return m * weno5(up ? s(f - 3) : s(f + 2), up ? s(f - 2) : s(f + 1), up ? s(f - 1) : s(f), up ? s(f) : s(f - 1),
+                     up ? s(f + 1) : s(f - 2), eps);
+  return m * vrecon(s, f, n, up, eps);
+}
+
 // ---------------------------------------------------------------------------------------------
 // thermodynamics
 // ---------------------------------------------------------------------------------------------

@@ -181,6 +181,17 @@ class Solver:
         check(self.lib.lexgb_check_finite(self.handle, ctypes.byref(n)))
         return n.value
 
+    def step_kernel_count(self):
+        n = ctypes.c_int()
+        check(self.lib.lexgb_step_kernel_count(self.handle, ctypes.byref(n)))
+        return n.value
+
+    def time_kernel(self, name, reps=20):
+        """Average duration [ms] of one launch of a step kernel, CUDA events on the solver's stream."""
+        ms = ctypes.c_float()
+        check(self.lib.lexgb_time_kernel(self.handle, _lib.KERNELS.index(name), int(reps), ctypes.byref(ms)))
+        return ms.value
+
     def device_ptrs(self):
         arr = (ctypes.c_void_p * 6)()
         check(self.lib.lexgb_state_device_ptrs(self.handle, arr))

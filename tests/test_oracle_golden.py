@@ -123,3 +123,15 @@ def test_oracle_fp32_mode_runs(ops_golden):
     ref = g["step_w"]
     assert all(np.all(np.isfinite(a)) for a in nxt)
     assert rel_l2(nxt[3], ref) < 1e-3
+
+
+def test_product_workload_matches_oracle_ic():
+    """lex_gb300.workload (product) builds the same initial state as the oracle's generator."""
+    from lex_gb300.workload import warm_bubble
+    wb = WarmBubble(20, 12, 10, 600.0, 600.0, 300.0, seed=5)
+    phys, base, _ = wb.build()
+    mine, prof = warm_bubble(20, 12, 10, 600.0, 600.0, 300.0, seed=5)
+    for a, b in zip(mine, phys):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(prof["theta0"], base[2][0, 0])
+    np.testing.assert_array_equal(prof["qv0"], base[4][0, 0])
