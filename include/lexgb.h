@@ -160,6 +160,23 @@ enum {
 };
 int lexgb_time_kernel(lexgb_ctx *ctx, int which, int reps, float *ms_per_launch);
 
+/* FP64 budgets without any device allocation (no counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc - code inside a framework that owns all device memory
+ * through its own pool, work being recorded into a CUDA graph, or a loop that cannot afford
+ * cudaMalloc's implicit synchronisation).  Same four sums as lexgb_budget, for a state the
+ * caller holds in device memory in the internal layout (see lexgb_state_device_ptrs: theta
+ * minus theta_ref, x fastest, w with nz+1 levels), FP64 padded base columns rho0 and pi0
+ * (nz+2, device) and a device output of 4 doubles; enqueued on `stream` (cudaStream_t, NULL =
+ * legacy default stream), not synchronised.  Partial sums go to a fixed array of
+ * LEXGB_NOALLOC_MAX_BLOCKS x 4 doubles (256 KiB) compiled into the library, one slot per 2048
+ * cells: grids above 16,777,216 cells are rejected with LEXGB_ERR_ARG.  The first call on a
+ * device looks up that array's device address (make it before any stream capture); all calls
+ * share the array, so calls that overlap on the GPU race. */
+#define LEXGB_NOALLOC_MAX_BLOCKS 8192
+int lexgb_budget_noalloc(int nx, int ny, int nz, double dx, double dy, double dz, double theta_ref,
+                         const float *const fields[6], const double *rho0_col, const double *pi0_col,
+                         double *out, void *stream);
+
 /* Message of the last failure on this thread; returns the untruncated length. */
 int lexgb_last_error(char *buf, size_t len);
 

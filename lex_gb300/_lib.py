@@ -51,6 +51,8 @@ SIGNATURES = {
     "lexgb_state_device_ptrs": (_I, [_P, ctypes.POINTER(_P)]),
     "lexgb_step_kernel_count": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
     "lexgb_time_kernel": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_float)]),
+    "lexgb_budget_noalloc": (_I, [_I, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  ctypes.POINTER(_P), _P, _P, _P, _P]),
     "lexgb_last_error": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
 }
 

@@ -40,6 +40,11 @@ constexpr int NFIELD = 6;  // T u v w p q
 
 }  // namespace
 
+namespace lexgb {
+// lets other translation units of the library report through lexgb_last_error
+void record_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace lexgb
+
 struct lexgb_ctx {
   lexgb_config cfg{};
   Dims d{};
