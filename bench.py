@@ -264,7 +264,7 @@ def run_lexgb(args):
     S.upload(phys, dtype=np.float32)
     S.step(2, graph=True)
     kern = {k: S.time_kernel(k, reps=32 if k == "acoustic" else 8) for k in
-            ("acoustic", "div_trho", "adv_scalars", "adv_u", "adv_v", "adv_w", "smag_a", "smag_b")}
+            ("acoustic", "div_trho", "adv_scalars", "adv_momentum", "smag_a", "smag_b")}
     peak, peak_kind = peaks()
     ac_ms = kern["acoustic"]
     achieved = B_ACOUSTIC * npts / (ac_ms * 1e-3) / 1e9

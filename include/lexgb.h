@@ -51,6 +51,7 @@ typedef struct lexgb_config {
     int cor_opt;             /* 0: none, 1: Coriolis, 2: Coriolis + large-scale pressure gradient */
     double f_cor;            /* Coriolis parameter (namelist_n_constants.py:39) */
     double theta_ref;        /* constant subtracted from theta on the device; 0 = use theta0 at the first level */
+    int acoustic_pairs;      /* 0 (default): one acoustic sub-step per launch; 1: two per launch (temporal blocking) */
 } lexgb_config;
 
 typedef struct lexgb_ctx lexgb_ctx;
@@ -151,11 +152,10 @@ enum {
     LEXGB_KERNEL_ACOUSTIC = 0,  /* one acoustic sub-step */
     LEXGB_KERNEL_DIV_TRHO,      /* mass divergence + theta_rho */
     LEXGB_KERNEL_ADV_SCALARS,   /* theta and qv advection + Euler update */
-    LEXGB_KERNEL_ADV_U,
-    LEXGB_KERNEL_ADV_V,
-    LEXGB_KERNEL_ADV_W,
+    LEXGB_KERNEL_ADV_MOMENTUM,  /* u, v, w advection + Coriolis + buoyancy + SGS -> R_u, R_v, R_w */
     LEXGB_KERNEL_SMAG_A,
     LEXGB_KERNEL_SMAG_B,
+    LEXGB_KERNEL_ACOUSTIC_PAIR, /* two acoustic sub-steps */
     LEXGB_KERNEL_COUNT
 };
 int lexgb_time_kernel(lexgb_ctx *ctx, int which, int reps, float *ms_per_launch);

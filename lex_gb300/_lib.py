@@ -16,7 +16,7 @@ DIAGNOSTICS = ["mass_div", "adv_theta", "adv_qv", "adv_u", "adv_v", "adv_w", "bu
                "pgf_u", "pgf_v", "pgf_w", "adv_pi", "sgs_u", "sgs_v", "sgs_w", "sgs_theta", "sgs_qv",
                "n2", "km"]
 
-KERNELS = ["acoustic", "div_trho", "adv_scalars", "adv_u", "adv_v", "adv_w", "smag_a", "smag_b"]
+KERNELS = ["acoustic", "div_trho", "adv_scalars", "adv_momentum", "smag_a", "smag_b", "acoustic_pair"]
 
 # every entry point include/lexgb.h declares: name -> (restype, argtypes)
 _P = ctypes.c_void_p
@@ -29,7 +29,8 @@ class Config(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
                 ("dt", ctypes.c_double), ("n_sound", ctypes.c_int), ("turb_opt", ctypes.c_int),
-                ("cor_opt", ctypes.c_int), ("f_cor", ctypes.c_double), ("theta_ref", ctypes.c_double)]
+                ("cor_opt", ctypes.c_int), ("f_cor", ctypes.c_double), ("theta_ref", ctypes.c_double),
+                ("acoustic_pairs", ctypes.c_int)]
 
 
 SIGNATURES = {

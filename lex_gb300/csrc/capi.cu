@@ -157,25 +157,30 @@ int run_stage(lexgb_ctx* c, int s, const State& xi0, const State& xis, const Sta
   if (sgs_on) sg = Sgs{c->sgs[0], c->sgs[1], c->sgs[2], c->sgs[3], c->sgs[4]};
   SlowOut so{nullptr, nullptr, nullptr, out.T, out.q, dT, dq};
   CK(launch_adv_scalars(c->d, c->ph, c->cols, xis, c->div, xi0.T, xi0.q, sg, (float)p.dts[s], so, c->stream));
-  CK(launch_adv_u(c->d, c->ph, c->cols, xis, c->div, sg.u, c->Ru, c->stream));
-  CK(launch_adv_v(c->d, c->ph, c->cols, xis, c->div, sg.v, c->Rv, c->stream));
-  CK(launch_adv_w(c->d, c->ph, c->cols, xis, c->div, sg.w, c->Rw, 0, c->stream));
-  // acoustic sub-steps from xi0's winds and pi'; pi'_s is the stage state's pi'
+  CK(launch_adv_momentum(c->d, c->ph, c->cols, xis, c->div, sg, c->Ru, c->Rv, c->Rw, 0, c->stream));
+  // acoustic sub-steps from xi0's winds and pi'; pi'_s is the stage state's pi'.  With
+  // acoustic_pairs, sub-steps go two per launch (an odd count starts with a single one).
   const int n = p.n[s];
   const float dtau = (float)p.dtau[s];
   AcousticIn in{xi0.u, xi0.v, xi0.w, xi0.p, c->Ru, c->Rv, c->Rw, c->trho, xis.p};
   const AcousticOut X{c->Xu, c->Xv, c->Xw, c->Xp}, Y{c->Yu, c->Yv, c->Yw, c->Yp};
   const AcousticOut O{out.u, out.v, out.w, out.p};
+  const bool pairs = c->cfg.acoustic_pairs != 0;
+  const int nsingle = pairs ? (n & 1) : n;
+  const int launches = nsingle + (pairs ? n / 2 : 0);
   const bool alias = (out.u == xi0.u);
-  for (int m = 1; m <= n; ++m) {
-    AcousticOut tgt = (m == n && !(alias && n == 1)) ? O : ((m & 1) ? X : Y);
-    CK(launch_acoustic(c->d, c->ph, c->cols, in, tgt, dtau, c->stream));
+  for (int l = 1; l <= launches; ++l) {
+    AcousticOut tgt = (l == launches && !(alias && launches == 1)) ? O : ((l & 1) ? X : Y);
+    if (l <= nsingle)
+      CK(launch_acoustic(c->d, c->ph, c->cols, in, tgt, dtau, c->stream));
+    else
+      CK(launch_acoustic_pair(c->d, c->ph, c->cols, in, tgt, dtau, c->stream));
     in.u = tgt.u;
     in.v = tgt.v;
     in.w = tgt.w;
     in.p = tgt.p;
   }
-  if (alias && n == 1) {  // single sub-step into the buffer it started from: stage through X
+  if (alias && launches == 1) {  // one launch into the buffer it started from: staged through X
     const size_t bytes = c->fstride * sizeof(float);
     CK(cudaMemcpyAsync(out.u, c->Xu, bytes, cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaMemcpyAsync(out.v, c->Xv, bytes, cudaMemcpyDeviceToDevice, c->stream));
@@ -277,6 +282,7 @@ int lexgb_default_config(lexgb_config* cfg) {
   cfg->cor_opt = 0;
   cfg->f_cor = 1.0e-4;
   cfg->theta_ref = 0.0;
+  cfg->acoustic_pairs = 0;
   return LEXGB_OK;
 }
 
@@ -293,6 +299,7 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
   if (cfg->turb_opt != 0 && cfg->turb_opt != 1)
     return fail(LEXGB_ERR_ARG, "turb_opt must be 0 or 1 (the anisotropic turb_opt=2 is not provided)");
   if (cfg->cor_opt < 0 || cfg->cor_opt > 2) return fail(LEXGB_ERR_ARG, "cor_opt must be 0, 1 or 2");
+  if (cfg->acoustic_pairs != 0 && cfg->acoustic_pairs != 1) return fail(LEXGB_ERR_ARG, "acoustic_pairs must be 0 or 1");
   lexgb_ctx* c = new lexgb_ctx();
   c->cfg = *cfg;
   c->d = Dims{cfg->nx, cfg->ny, cfg->nz};
@@ -314,6 +321,9 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
   };
   cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
+  e = init_weno_attributes();
+  if (e == cudaSuccess) e = init_acoustic_attributes();
+  if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("kernel attributes: ") + cudaGetErrorString(e));
   c->stream = c->own_stream;
   // 3 states + 2 acoustic ping-pong sets + R(3) + trho + div + sgs(5) + tau(7) + diag(3)
   c->arena_fields = 3 * NFIELD + 8 + 5 + 5 + 7 + 3;
@@ -551,10 +561,15 @@ int lexgb_diagnose(lexgb_ctx* c, int what, double* host_out) {
       out = what == LEXGB_DIAG_ADV_THETA ? c->diag[0] : c->diag[1];
       break;
     }
-    case LEXGB_DIAG_ADV_U: CK(launch_adv_u(d, ph, c->cols, c->A, c->div, nullptr, out, c->stream)); kind = 1; break;
-    case LEXGB_DIAG_ADV_V: CK(launch_adv_v(d, ph, c->cols, c->A, c->div, nullptr, out, c->stream)); kind = 2; break;
-    case LEXGB_DIAG_ADV_W: CK(launch_adv_w(d, ph, c->cols, c->A, c->div, nullptr, out, 1, c->stream)); kind = 3; break;
-    case LEXGB_DIAG_BUOY_W: CK(launch_adv_w(d, ph, c->cols, c->A, c->div, nullptr, out, 2, c->stream)); kind = 3; break;
+    case LEXGB_DIAG_ADV_U:
+    case LEXGB_DIAG_ADV_V:
+    case LEXGB_DIAG_ADV_W:
+    case LEXGB_DIAG_BUOY_W:
+      CK(launch_adv_momentum(d, ph, c->cols, c->A, c->div, none, c->diag[0], c->diag[1], c->diag[2],
+                             what == LEXGB_DIAG_BUOY_W ? 2 : 1, c->stream));
+      kind = what == LEXGB_DIAG_ADV_U ? 1 : (what == LEXGB_DIAG_ADV_V ? 2 : 3);
+      out = c->diag[kind - 1];
+      break;
     case LEXGB_DIAG_PGF_U:
     case LEXGB_DIAG_PGF_V:
     case LEXGB_DIAG_PGF_W:
@@ -670,12 +685,17 @@ int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
         in.u = o.u; in.v = o.v; in.w = o.w; in.p = o.p;
         return e;
       }
+      case LEXGB_KERNEL_ACOUSTIC_PAIR: {
+        const AcousticOut o = (r & 1) ? Y : X;
+        cudaError_t e = launch_acoustic_pair(d, c->ph, c->cols, in, o, (float)p.dtau[2], c->stream);
+        in.u = o.u; in.v = o.v; in.w = o.w; in.p = o.p;
+        return e;
+      }
       case LEXGB_KERNEL_DIV_TRHO: return launch_div_trho(d, c->ph, c->cols, x, c->div, c->trho, c->stream);
       case LEXGB_KERNEL_ADV_SCALARS:
         return launch_adv_scalars(d, c->ph, c->cols, x, c->div, x.T, x.q, sg, (float)p.dts[2], so, c->stream);
-      case LEXGB_KERNEL_ADV_U: return launch_adv_u(d, c->ph, c->cols, x, c->div, sg.u, c->Ru, c->stream);
-      case LEXGB_KERNEL_ADV_V: return launch_adv_v(d, c->ph, c->cols, x, c->div, sg.v, c->Rv, c->stream);
-      case LEXGB_KERNEL_ADV_W: return launch_adv_w(d, c->ph, c->cols, x, c->div, sg.w, c->Rw, 0, c->stream);
+      case LEXGB_KERNEL_ADV_MOMENTUM:
+        return launch_adv_momentum(d, c->ph, c->cols, x, c->div, sg, c->Ru, c->Rv, c->Rw, 0, c->stream);
       case LEXGB_KERNEL_SMAG_A: return launch_smag_a(d, c->ph, c->cols, x, t, c->stream);
       default: {
         SgsOut o{c->sgs[0], c->sgs[1], c->sgs[2], c->sgs[3], c->sgs[4]};
@@ -685,9 +705,10 @@ int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
   };
   // populate every input the timed kernel reads, then warm up once
   CK(launch_smag_a(d, c->ph, c->cols, x, t, c->stream));
-  CK(launch_adv_u(d, c->ph, c->cols, x, c->div, nullptr, c->Ru, c->stream));
-  CK(launch_adv_v(d, c->ph, c->cols, x, c->div, nullptr, c->Rv, c->stream));
-  CK(launch_adv_w(d, c->ph, c->cols, x, c->div, nullptr, c->Rw, 0, c->stream));
+  {
+    const Sgs none{nullptr, nullptr, nullptr, nullptr, nullptr};
+    CK(launch_adv_momentum(d, c->ph, c->cols, x, c->div, none, c->Ru, c->Rv, c->Rw, 0, c->stream));
+  }
   CK(launch(0));
   in = AcousticIn{x.u, x.v, x.w, x.p, c->Ru, c->Rv, c->Rw, c->trho, x.p};
   cudaEvent_t e0, e1;

@@ -176,6 +176,273 @@ __global__ void __launch_bounds__(256) k_acoustic4(Dims d, Phys ph, Cols c, Acou
   if (k == nz - 1) *reinterpret_cast<float4*>(o.w + rt + i0) = z4;
 }
 
+// ================================================================================================
+// Two sub-steps per launch (temporal blocking).
+//
+// A block owns a 32 x 4 x 4 tile T of cells.  The first sub-step is evaluated on T grown by one
+// cell on every side (E), which is exactly what the second sub-step reads, so the two sub-steps
+// need their inputs once: pi', theta_rho and pi'_s on T grown by two cells (boxes), and the
+// winds and slow tendencies on the faces of E.  Each field crosses DRAM once per two sub-steps.
+//
+// Phases (one __syncthreads between each):
+//   0  stage the boxes; every thread also loads the old winds and R of the faces it owns
+//   1  winds after sub-step 1 on all faces of E               -> uf / vf / wf
+//   2  pi' after sub-step 1 on the cells of E                 -> pm
+//   3  winds after sub-step 2 on the faces of T (in place in uf / vf / wf; own faces stored)
+//   4  pi' after sub-step 2 on T (stored)
+// ================================================================================================
+namespace tb {
+constexpr int TX = 32, TY = 4, TZ = 4, NT = TX * TY * TZ;
+constexpr int EX = TX + 2, EY = TY + 2, EZ = TZ + 2;  // E: cells i0-1 .. i0+TX
+constexpr int HBX = TX + 4, HBY = TY + 4, HBZ = TZ + 4;  // boxes: cells i0-2 .. i0+TX+1
+constexpr int NU = (EX + 1) * EY * EZ;                // x faces of E
+constexpr int NV = EX * (EY + 1) * EZ;                // y faces of E
+constexpr int NW = EX * EY * (EZ + 1);                // z faces of E
+constexpr int IU = (NU + NT - 1) / NT, IV = (NV + NT - 1) / NT, IW = (NW + NT - 1) / NT;
+constexpr int NB = HBX * HBY * HBZ;
+constexpr int IB = (NB + NT - 1) / NT;
+
+struct Smem {
+  float P[HBZ][HBY][HBX], TR[HBZ][HBY][HBX], PS[HBZ][HBY][HBX];
+  float uf[EZ][EY][EX + 1];  // u on x faces i0-1+f
+  float vf[EZ][EY + 1][EX];  // v on y faces j0-1+f
+  float wf[EZ + 1][EY][EX];  // w on z faces k0-1+f
+  float pm[EZ][EY][EX];      // pi' after sub-step 1 on E
+  int gx[HBX];                // x index of box column (i0-2+b), wrapped
+  int gy[HBY];                // (j0-2+b) wrapped, times nx
+  int gz[HBZ];                // (k0-2+b) clamped to 0..nz-1, times nx*ny
+};
+}  // namespace tb
+
+__global__ void __launch_bounds__(tb::NT) k_acoustic_pair(Dims d, Phys ph, Cols c, AcousticIn a, AcousticOut o,
+                                                        float dtau) {
+  using namespace tb;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
+  const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
+  const int tid = threadIdx.x;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * TZ;
+  if (tid < HBX) {
+    int i = (i0 - 2 + tid) % nx;
+    S.gx[tid] = i < 0 ? i + nx : i;
+  } else if (tid < HBX + HBY) {
+    int j = (j0 - 2 + (tid - HBX)) % ny;
+    S.gy[tid - HBX] = (j < 0 ? j + ny : j) * nx;
+  } else if (tid < HBX + HBY + HBZ) {
+    S.gz[tid - HBX - HBY] = clampi(k0 - 2 + (tid - HBX - HBY), 0, nz - 1) * plane;
+  }
+  __syncthreads();
+
+  // ---------------------------------------------------------------- phase 0: loads
+  float stP[IB], stT[IB], stS[IB];
+#pragma unroll
+  for (int q = 0; q < IB; ++q) {
+    const int t = tid + q * NT;
+    if (t < NB) {
+      const int bx = t % HBX, by = (t / HBX) % HBY, bz = t / (HBX * HBY);
+      const int g = S.gz[bz] + S.gy[by] + S.gx[bx];
+      stP[q] = __ldg(a.p + g);
+      stT[q] = __ldg(a.trho + g);
+      stS[q] = __ldg(a.ps + g);
+    }
+  }
+  // owned faces: x face item t -> (f, ey, ez) with global face i0-1+f, row j0-1+ey, level k0-1+ez
+  float u0[IU], ru[IU], v0[IV], rv[IV], w0[IW], rw[IW];
+#pragma unroll
+  for (int q = 0; q < IU; ++q) {
+    const int t = tid + q * NT;
+    u0[q] = ru[q] = 0.f;
+    if (t < NU) {
+      const int f = t % (EX + 1), ey = (t / (EX + 1)) % EY, ez = t / ((EX + 1) * EY);
+      const int k = k0 - 1 + ez;
+      if (k >= 0 && k < nz) {
+        const int g = S.gz[ez + 1] + S.gy[ey + 1] + S.gx[f + 1];
+        u0[q] = __ldg(a.u + g);
+        ru[q] = __ldg(a.Ru + g);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < IV; ++q) {
+    const int t = tid + q * NT;
+    v0[q] = rv[q] = 0.f;
+    if (t < NV) {
+      const int ex = t % EX, f = (t / EX) % (EY + 1), ez = t / (EX * (EY + 1));
+      const int k = k0 - 1 + ez;
+      if (k >= 0 && k < nz) {
+        const int g = S.gz[ez + 1] + S.gy[f + 1] + S.gx[ex + 1];
+        v0[q] = __ldg(a.v + g);
+        rv[q] = __ldg(a.Rv + g);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < IW; ++q) {
+    const int t = tid + q * NT;
+    w0[q] = rw[q] = 0.f;
+    if (t < NW) {
+      const int ex = t % EX, ey = (t / EX) % EY, f = t / (EX * EY);
+      const int kf = k0 - 1 + f;  // face level
+      if (kf > 0 && kf < nz) {
+        const int g = kf * plane + S.gy[ey + 1] + S.gx[ex + 1];
+        w0[q] = __ldg(a.w + g);
+        rw[q] = __ldg(a.Rw + g);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < IB; ++q) {
+    const int t = tid + q * NT;
+    if (t < NB) {
+      (&S.P[0][0][0])[t] = stP[q];
+      (&S.TR[0][0][0])[t] = stT[q];
+      (&S.PS[0][0][0])[t] = stS[q];
+    }
+  }
+  __syncthreads();
+
+  // ---------------------------------------------------------------- phase 1: winds after sub-step 1 on E
+#pragma unroll
+  for (int q = 0; q < IU; ++q) {
+    const int t = tid + q * NT;
+    if (t < NU) {
+      const int f = t % (EX + 1), ey = (t / (EX + 1)) % EY, ez = t / ((EX + 1) * EY);
+      const int bx = f + 1, by = ey + 1, bz = ez + 1;  // box cell right of the face
+      const float g = pgf(S.TR[bz][by][bx], S.TR[bz][by][bx - 1], S.P[bz][by][bx], S.P[bz][by][bx - 1], ph.rdx);
+      (&S.uf[0][0][0])[t] = u0[q] + (g + ru[q]) * dtau;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < IV; ++q) {
+    const int t = tid + q * NT;
+    if (t < NV) {
+      const int ex = t % EX, f = (t / EX) % (EY + 1), ez = t / (EX * (EY + 1));
+      const int bx = ex + 1, by = f + 1, bz = ez + 1;
+      const float g = pgf(S.TR[bz][by][bx], S.TR[bz][by - 1][bx], S.P[bz][by][bx], S.P[bz][by - 1][bx], ph.rdy);
+      (&S.vf[0][0][0])[t] = v0[q] + (g + rv[q]) * dtau;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < IW; ++q) {
+    const int t = tid + q * NT;
+    if (t < NW) {
+      const int ex = t % EX, ey = (t / EX) % EY, f = t / (EX * EY);
+      const int kf = k0 - 1 + f;
+      float wn = 0.f;
+      if (kf > 0 && kf < nz) {
+        const int bx = ex + 1, by = ey + 1, bz = f + 1;
+        const float g = pgf(S.TR[bz][by][bx], S.TR[bz - 1][by][bx], S.P[bz][by][bx], S.P[bz - 1][by][bx], ph.rdz);
+        wn = w0[q] + (g + rw[q]) * dtau;
+      }
+      (&S.wf[0][0][0])[t] = wn;
+    }
+  }
+  __syncthreads();
+
+  // ---------------------------------------------------------------- phase 2: pi' after sub-step 1 on E
+  constexpr int NE = EX * EY * EZ;
+  for (int t = tid; t < NE; t += NT) {
+    const int ex = t % EX, ey = (t / EX) % EY, ez = t / (EX * EY);
+    const int k = k0 - 1 + ez;
+    if (k < 0 || k >= nz) continue;
+    const int bx = ex + 1, by = ey + 1, bz = ez + 1;
+    const float uw = S.uf[ez][ey][ex], ue = S.uf[ez][ey][ex + 1];
+    const float vs = S.vf[ez][ey][ex], vn = S.vf[ez][ey + 1][ex];
+    const float wb = S.wf[ez][ey][ex], wt = S.wf[ez + 1][ey][ex];
+    const float div = (ue - uw) * ph.rdx + (vn - vs) * ph.rdy + (wt - wb) * ph.rdz;
+    const float s0 = S.PS[bz][by][bx];
+    const float gxw = (s0 - S.PS[bz][by][bx - 1]) * ph.rdx, gxe = (S.PS[bz][by][bx + 1] - s0) * ph.rdx;
+    const float gys = (s0 - S.PS[bz][by - 1][bx]) * ph.rdy, gyn = (S.PS[bz][by + 1][bx] - s0) * ph.rdy;
+    const float wzb = (k == 0) ? 0.f : wb * (c.dpi0dz[k] + (s0 - S.PS[bz - 1][by][bx]) * ph.rdz);
+    const float wzt = (k + 1 >= nz) ? 0.f : wt * (c.dpi0dz[k + 1] + (S.PS[bz + 1][by][bx] - s0) * ph.rdz);
+    const float ap = -(0.5f * (ue * gxe + uw * gxw) + 0.5f * (vn * gyn + vs * gys) +
+                       (0.5f * wzb * c.rho_face[k] + 0.5f * wzt * c.rho_face[k + 1]) / c.rho[k]);
+    const float dpdt = -kRdCv * ((c.pi0[k] + s0) * div) + ap;
+    S.pm[ez][ey][ex] = S.P[bz][by][bx] + (kDivDamp * dpdt) * dtau;
+  }
+  __syncthreads();
+
+  // ---------------------------------------------------------------- phase 3: winds after sub-step 2 on T
+#pragma unroll
+  for (int q = 0; q < IU; ++q) {
+    const int t = tid + q * NT;
+    if (t < NU) {
+      const int f = t % (EX + 1), ey = (t / (EX + 1)) % EY, ez = t / ((EX + 1) * EY);
+      if (f >= 1 && f <= TX + 1 && ey >= 1 && ey <= TY && ez >= 1 && ez <= TZ) {
+        const int k = k0 - 1 + ez;
+        if (k < nz) {
+          const int bx = f + 1, by = ey + 1, bz = ez + 1;
+          const float g = pgf(S.TR[bz][by][bx], S.TR[bz][by][bx - 1], S.pm[ez][ey][f], S.pm[ez][ey][f - 1], ph.rdx);
+          const float un = S.uf[ez][ey][f] + (g + ru[q]) * dtau;
+          S.uf[ez][ey][f] = un;
+          const int i = i0 - 1 + f, j = j0 - 1 + ey;
+          if (f <= TX && i < nx && j < ny) o.u[k * plane + j * nx + i] = un;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < IV; ++q) {
+    const int t = tid + q * NT;
+    if (t < NV) {
+      const int ex = t % EX, f = (t / EX) % (EY + 1), ez = t / (EX * (EY + 1));
+      if (ex >= 1 && ex <= TX && f >= 1 && f <= TY + 1 && ez >= 1 && ez <= TZ) {
+        const int k = k0 - 1 + ez;
+        if (k < nz) {
+          const int bx = ex + 1, by = f + 1, bz = ez + 1;
+          const float g = pgf(S.TR[bz][by][bx], S.TR[bz][by - 1][bx], S.pm[ez][f][ex], S.pm[ez][f - 1][ex], ph.rdy);
+          const float vn = S.vf[ez][f][ex] + (g + rv[q]) * dtau;
+          S.vf[ez][f][ex] = vn;
+          const int i = i0 - 1 + ex, j = j0 - 1 + f;
+          if (f <= TY && i < nx && j < ny) o.v[k * plane + j * nx + i] = vn;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < IW; ++q) {
+    const int t = tid + q * NT;
+    if (t < NW) {
+      const int ex = t % EX, ey = (t / EX) % EY, f = t / (EX * EY);
+      if (ex >= 1 && ex <= TX && ey >= 1 && ey <= TY && f >= 1 && f <= TZ + 1) {
+        const int kf = k0 - 1 + f;
+        float wn = 0.f;
+        if (kf > 0 && kf < nz) {
+          const int bx = ex + 1, by = ey + 1, bz = f + 1;
+          const float g = pgf(S.TR[bz][by][bx], S.TR[bz - 1][by][bx], S.pm[f][ey][ex], S.pm[f - 1][ey][ex], ph.rdz);
+          wn = S.wf[f][ey][ex] + (g + rw[q]) * dtau;
+        }
+        S.wf[f][ey][ex] = wn;
+        const int i = i0 - 1 + ex, j = j0 - 1 + ey;
+        if (i < nx && j < ny && kf <= nz && (f <= TZ || kf == nz)) o.w[kf * plane + j * nx + i] = wn;
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---------------------------------------------------------------- phase 4: pi' after sub-step 2 on T
+  {
+    const int tx = tid % TX, ty = (tid / TX) % TY, tz = tid / (TX * TY);
+    const int i = i0 + tx, j = j0 + ty, k = k0 + tz;
+    if (i >= nx || j >= ny || k >= nz) return;
+    const int ex = tx + 1, ey = ty + 1, ez = tz + 1;
+    const int bx = tx + 2, by = ty + 2, bz = tz + 2;
+    const float uw = S.uf[ez][ey][ex], ue = S.uf[ez][ey][ex + 1];
+    const float vs = S.vf[ez][ey][ex], vn = S.vf[ez][ey + 1][ex];
+    const float wb = S.wf[ez][ey][ex], wt = S.wf[ez + 1][ey][ex];
+    const float div = (ue - uw) * ph.rdx + (vn - vs) * ph.rdy + (wt - wb) * ph.rdz;
+    const float s0 = S.PS[bz][by][bx];
+    const float gxw = (s0 - S.PS[bz][by][bx - 1]) * ph.rdx, gxe = (S.PS[bz][by][bx + 1] - s0) * ph.rdx;
+    const float gys = (s0 - S.PS[bz][by - 1][bx]) * ph.rdy, gyn = (S.PS[bz][by + 1][bx] - s0) * ph.rdy;
+    const float wzb = (k == 0) ? 0.f : wb * (c.dpi0dz[k] + (s0 - S.PS[bz - 1][by][bx]) * ph.rdz);
+    const float wzt = (k + 1 >= nz) ? 0.f : wt * (c.dpi0dz[k + 1] + (S.PS[bz + 1][by][bx] - s0) * ph.rdz);
+    const float ap = -(0.5f * (ue * gxe + uw * gxw) + 0.5f * (vn * gyn + vs * gys) +
+                       (0.5f * wzb * c.rho_face[k] + 0.5f * wzt * c.rho_face[k + 1]) / c.rho[k]);
+    const float dpdt = -kRdCv * ((c.pi0[k] + s0) * div) + ap;
+    o.p[k * plane + j * nx + i] = S.pm[ez][ey][ex] + (kDivDamp * dpdt) * dtau;
+  }
+}
+
 __global__ void k_diag_pgf(Dims d, Phys ph, Cols c, const float* __restrict__ p, const float* __restrict__ trho,
                            float* pu, float* pv, float* pw) {
   const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y, f = blockIdx.z * BZ + threadIdx.z;
@@ -219,6 +486,17 @@ cudaError_t launch_acoustic(const Dims& d, const Phys& ph, const Cols& c, Acoust
   dim3 g((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, (d.nz + BZ - 1) / BZ);
   k_acoustic<<<g, dim3(BX, BY, BZ), 0, st>>>(d, ph, c, in, out, dtau);
   return cudaGetLastError();
+}
+
+cudaError_t launch_acoustic_pair(const Dims& d, const Phys& ph, const Cols& c, AcousticIn in, AcousticOut out,
+                                 float dtau, cudaStream_t st) {
+  dim3 g((d.nx + tb::TX - 1) / tb::TX, (d.ny + tb::TY - 1) / tb::TY, (d.nz + tb::TZ - 1) / tb::TZ);
+  k_acoustic_pair<<<g, tb::NT, sizeof(tb::Smem), st>>>(d, ph, c, in, out, dtau);
+  return cudaGetLastError();
+}
+
+cudaError_t init_acoustic_attributes() {
+  return cudaFuncSetAttribute(k_acoustic_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(tb::Smem));
 }
 
 cudaError_t launch_diag_pgf(const Dims& d, const Phys& ph, const Cols& c, const float* p, const float* trho,

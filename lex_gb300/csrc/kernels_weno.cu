@@ -1,0 +1,466 @@
+// kernels_weno.cu - slow-mode WENO5 advection of one RK stage, tiled in 3-D.
+//
+// Flux-form advection of the prognostic fields (advection.py:9-149, fluxes :305-1281):
+//
+//   tendency(phi) = ( -sum_d d(m_d * phi_face)/dx_d + phi * div_at_phi ) / rho_at_phi
+//
+// Two kernels: k_weno_scalars advects theta and qv together (their mass fluxes are the same
+// rho0*u, rho0*v, rho0*w on the cell faces), k_weno_momentum advects u, v and w together (their
+// mass fluxes are averages of the three winds, all staged in shared memory).
+//
+// A block owns a 32 x 4 x 4 box of points, one thread per point.  It stages each field on the
+// box plus a 3-cell halo in shared memory (periodic in x and y, clamped in z), evaluates every x,
+// y and z face flux of the box exactly once - each thread its point's west, south and bottom
+// faces, whole warps the box's north, top and east edge faces - and forms each point's tendency
+// from its six face fluxes.  The upwind stencil is selected from the sign of the mass flux
+// before the reconstruction.  Global indices of the halo coordinates are tabulated per block.
+//
+// Outputs (one_step_integration.py:258-296):
+//   theta, qv : phi_next = phi^0 + dt_s * adv (+ dt_s * sgs); optional record of adv (+ sgs)
+//   u         : R_u = adv + f v (Coriolis, pressure_gradient_coriolis.py:80-113) + sgs_u
+//   v         : R_v = adv - f u + sgs_v
+//   w         : R_w = adv + b8w (buoyancy at faces, pressure_equations.py:162-172) + sgs_w, with
+//               adv = 0 on the bottom and lid faces (advection.py:146-147); wmode 1: adv only,
+//               wmode 2: b8w only (diagnostics).
+#include "lexgb_internal.cuh"
+
+namespace lexgb {
+
+namespace {
+
+constexpr int TX = 32, TY = 4, TZ = 4, HALO = 3;
+constexpr int NT = TX * TY * TZ;
+constexpr int BX3 = TX + 2 * HALO, BY3 = TY + 2 * HALO, BZ3 = TZ + 2 * HALO;
+
+typedef float Box[BZ3][BY3][BX3];
+typedef float FluxX[TZ][TY][TX + 1];
+typedef float FluxY[TZ][TY + 1][TX];
+typedef float FluxZ[TZ + 1][TY][TX];
+
+__device__ __forceinline__ int pmod(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+#define LD(p, idx) __ldg((p) + (idx))
+
+// global index tables of the box's halo coordinates
+struct Idx {
+  int x[BX3];   // x index of box column lx
+  int y[BY3];   // y index of box row ly, times nx
+  int zc[BZ3];  // cell level of box layer lz clamped to 0..nz-1, times nx*ny
+  int zw[BZ3];  // face level clamped to 0..nz, times nx*ny
+  int zl[BZ3];  // unclamped level k0 - 3 + lz
+};
+
+__device__ __forceinline__ void build_idx(Idx& ix, int tid, int i0, int j0, int k0, const Dims& d) {
+  if (tid < BX3) {
+    ix.x[tid] = pmod(i0 - HALO + tid, d.nx);
+  } else if (tid < BX3 + BY3) {
+    ix.y[tid - BX3] = pmod(j0 - HALO + (tid - BX3), d.ny) * d.nx;
+  } else if (tid < BX3 + BY3 + BZ3) {
+    const int lz = tid - BX3 - BY3;
+    const int k = k0 - HALO + lz;
+    ix.zl[lz] = k;
+    ix.zc[lz] = clampi(k, 0, d.nz - 1) * d.plane();
+    ix.zw[lz] = clampi(k, 0, d.nz) * d.plane();
+  }
+}
+
+// Warp-per-row staging of NF fields on their boxes: warp w loads box rows w, w + 16, ... of every
+// field (lanes cover x; lanes 0..5 also the last 6 columns).  All loads are issued before any
+// shared-memory store, so a block pays one memory latency for its whole staging.
+constexpr int NWARP = NT / 32;
+constexpr int ROWS = BY3 * BZ3;
+constexpr int RPW = (ROWS + NWARP - 1) / NWARP;
+
+template <int NF>
+__device__ __forceinline__ void stage(Box* const (&b)[NF], const float* const (&f)[NF], const int* const (&zbase)[NF],
+                                      const Idx& ix, int warp, int lane) {
+  const int xa = ix.x[lane];
+  const bool tail = lane < BX3 - 32;
+  const int xb = tail ? ix.x[32 + lane] : 0;
+  float va[NF][RPW], vb[NF][RPW];
+#pragma unroll
+  for (int q = 0; q < RPW; ++q) {
+    const int r = warp + q * NWARP;
+    if (r < ROWS) {
+      const int lz = r / BY3, ly = r - lz * BY3;
+#pragma unroll
+      for (int n = 0; n < NF; ++n) {
+        const int base = zbase[n][lz] + ix.y[ly];
+        va[n][q] = LD(f[n], base + xa);
+        vb[n][q] = tail ? LD(f[n], base + xb) : 0.f;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < RPW; ++q) {
+    const int r = warp + q * NWARP;
+    if (r < ROWS) {
+      const int lz = r / BY3, ly = r - lz * BY3;
+#pragma unroll
+      for (int n = 0; n < NF; ++n) {
+        (*b[n])[lz][ly][lane] = va[n][q];
+        if (tail) (*b[n])[lz][ly][32 + lane] = vb[n][q];
+      }
+    }
+  }
+}
+
+// face value through column face H (between entries H-1 and H of an n-entry column), given
+// s(H-3..H+2); entries outside 0..n-1 are never used; zero on the end faces.  Near-boundary
+// rules of vertical_flux_scalar2 and friends (advection.py:327-406).
+__device__ __forceinline__ float vflux6(float m, float sm3, float sm2, float sm1, float s0, float sp1, float sp2, int H,
+                                        int n, float eps) {
+  if (H <= 0 || H >= n) return 0.f;
+  const bool up = m >= 0.f;
+  float r;
+  if (H >= 3 && H <= n - 3) {
+    r = weno5(up ? sm3 : sp2, up ? sm2 : sp1, up ? sm1 : s0, up ? s0 : sm1, up ? sp1 : sm2, eps);
+  } else if (up) {
+    if (H == 1)
+      r = 0.5f * (sm1 + s0);
+    else if (H == 2 || H == n - 1)
+      r = weno3(sm2, sm1, s0, eps);
+    else  // H == n-2
+      r = weno5(sm3, sm2, sm1, s0, sp1, eps);
+  } else {
+    if (H == n - 1)
+      r = 0.5f * (s0 + sm1);
+    else if (H == 1 || H == n - 2)
+      r = weno3(sp1, s0, sm1, eps);
+    else  // H == 2
+      r = weno5(sp2, sp1, s0, sm1, sm2, eps);
+  }
+  return m * r;
+}
+
+// WENO face fluxes of a staged field: box coordinates (lx, ly, lz) of the point right of / above
+// the face
+__device__ __forceinline__ float wx(const Box& b, int lx, int ly, int lz, float m, float eps) {
+  return weno_flux(m, b[lz][ly][lx - 3], b[lz][ly][lx - 2], b[lz][ly][lx - 1], b[lz][ly][lx], b[lz][ly][lx + 1],
+                   b[lz][ly][lx + 2], eps);
+}
+__device__ __forceinline__ float wy(const Box& b, int lx, int ly, int lz, float m, float eps) {
+  return weno_flux(m, b[lz][ly - 3][lx], b[lz][ly - 2][lx], b[lz][ly - 1][lx], b[lz][ly][lx], b[lz][ly + 1][lx],
+                   b[lz][ly + 2][lx], eps);
+}
+__device__ __forceinline__ float wz(const Box& b, int lx, int ly, int lz, float m, int H, int n, float eps) {
+  return vflux6(m, b[lz - 3][ly][lx], b[lz - 2][ly][lx], b[lz - 1][ly][lx], b[lz][ly][lx], b[lz + 1][ly][lx],
+                b[lz + 2][ly][lx], H, n, eps);
+}
+
+// ================================================================================================
+// theta and qv
+// ================================================================================================
+struct ScalarArgs {
+  const float* div;
+  const float* T0;  // values at the start of the big step (may alias the outputs)
+  const float* q0;
+  const float* sgsT;
+  const float* sgsQ;
+  float* Tn;
+  float* qn;
+  float* recT;
+  float* recQ;
+  float dts;
+};
+
+// the three face fluxes (x, y, z) of both scalars through the faces whose right/upper point is
+// box (lx, ly, lz); `which` selects x (0), y (1) or z (2)
+__device__ __forceinline__ void scalar_face(const Box& bT, const Box& bQ, const Cols& c, const State& s, const Idx& ix,
+                                            int which, int lx, int ly, int lz, int nz, float& fT, float& fQ) {
+  fT = 0.f;
+  fQ = 0.f;
+  const int k = ix.zl[lz];
+  if (which < 2) {
+    if (k < 0 || k >= nz) return;
+    const int g = ix.zc[lz] + ix.y[ly] + ix.x[lx];
+    if (which == 0) {
+      const float m = c.rho[k] * LD(s.u, g);
+      fT = wx(bT, lx, ly, lz, m, kWepsTheta);
+      fQ = wx(bQ, lx, ly, lz, m, kWepsQv);
+    } else {
+      const float m = c.rho[k] * LD(s.v, g);
+      fT = wy(bT, lx, ly, lz, m, kWepsTheta);
+      fQ = wy(bQ, lx, ly, lz, m, kWepsQv);
+    }
+  } else {
+    const int H = k;  // bottom face of level k; zero on the surface (sfc flux 0) and the lid
+    if (H < 1 || H >= nz) return;
+    const float m = c.rho_face[H] * LD(s.w, ix.zw[lz] + ix.y[ly] + ix.x[lx]);
+    fT = wz(bT, lx, ly, lz, m, H, nz, kWepsTheta);
+    fQ = wz(bQ, lx, ly, lz, m, H, nz, kWepsQv);
+  }
+}
+
+__global__ void __launch_bounds__(NT) k_weno_scalars(Dims d, Phys ph, Cols c, State s, ScalarArgs a) {
+  __shared__ Box bT, bQ;
+  __shared__ FluxX xT, xQ;
+  __shared__ FluxY yT, yQ;
+  __shared__ FluxZ zT, zQ;
+  __shared__ Idx ix;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
+  const int tid = (tz * TY + ty) * TX + tx, warp = tid >> 5;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * TZ;
+  build_idx(ix, tid, i0, j0, k0, d);
+  __syncthreads();
+  {
+    Box* const boxes[2] = {&bT, &bQ};
+    const float* const src[2] = {s.T, s.q};
+    const int* const zb[2] = {ix.zc, ix.zc};
+    stage<2>(boxes, src, zb, ix, warp, tx);
+  }
+  const int lx = tx + HALO, ly = ty + HALO, lz = tz + HALO;
+  const int k = k0 + tz;
+  const bool own = (i0 + tx < nx) && (j0 + ty < ny) && (k < nz);
+  const int id = k * d.plane() + ix.y[ly] + ix.x[lx];
+  float dv = 0.f, sT = 0.f, sQ = 0.f, T0 = 0.f, Q0 = 0.f;
+  if (own) {
+    dv = LD(a.div, id);
+    if (a.sgsT) {
+      sT = LD(a.sgsT, id);
+      sQ = LD(a.sgsQ, id);
+    }
+    T0 = a.T0[id];  // may alias the output: plain loads, same thread
+    Q0 = a.q0[id];
+  }
+  __syncthreads();
+  scalar_face(bT, bQ, c, s, ix, 0, lx, ly, lz, nz, xT[tz][ty][tx], xQ[tz][ty][tx]);
+  scalar_face(bT, bQ, c, s, ix, 1, lx, ly, lz, nz, yT[tz][ty][tx], yQ[tz][ty][tx]);
+  scalar_face(bT, bQ, c, s, ix, 2, lx, ly, lz, nz, zT[tz][ty][tx], zQ[tz][ty][tx]);
+  if (warp < 4) {  // north faces of layer `warp`
+    scalar_face(bT, bQ, c, s, ix, 1, lx, TY + HALO, warp + HALO, nz, yT[warp][TY][tx], yQ[warp][TY][tx]);
+  } else if (warp < 8) {  // top faces of row warp-4
+    const int ey = warp - 4;
+    scalar_face(bT, bQ, c, s, ix, 2, lx, ey + HALO, TZ + HALO, nz, zT[TZ][ey][tx], zQ[TZ][ey][tx]);
+  } else if (warp == 8 && tx < TY * TZ) {  // east faces
+    const int ey = tx % TY, ez = tx / TY;
+    scalar_face(bT, bQ, c, s, ix, 0, TX + HALO, ey + HALO, ez + HALO, nz, xT[ez][ey][TX], xQ[ez][ey][TX]);
+  }
+  __syncthreads();
+  if (!own) return;
+  const float r = c.rho[k];
+  const float cT = -((xT[tz][ty][tx + 1] - xT[tz][ty][tx]) * ph.rdx + (yT[tz][ty + 1][tx] - yT[tz][ty][tx]) * ph.rdy +
+                     (zT[tz + 1][ty][tx] - zT[tz][ty][tx]) * ph.rdz);
+  const float cQ = -((xQ[tz][ty][tx + 1] - xQ[tz][ty][tx]) * ph.rdx + (yQ[tz][ty + 1][tx] - yQ[tz][ty][tx]) * ph.rdy +
+                     (zQ[tz + 1][ty][tx] - zQ[tz][ty][tx]) * ph.rdz);
+  const float aT = (cT + bT[lz][ly][lx] * dv) / r;
+  const float aQ = (cQ + bQ[lz][ly][lx] * dv) / r;
+  float Tn = T0 + aT * a.dts, Qn = Q0 + aQ * a.dts, rT = aT, rQ = aQ;
+  if (a.sgsT) {
+    Tn = Tn + sT * a.dts;
+    Qn = Qn + sQ * a.dts;
+    rT = rT + sT;
+    rQ = rQ + sQ;
+  }
+  if (a.Tn) a.Tn[id] = Tn;
+  if (a.qn) a.qn[id] = Qn;
+  if (a.recT) a.recT[id] = rT;
+  if (a.recQ) a.recQ[id] = rQ;
+}
+
+// ================================================================================================
+// u, v, w
+// ================================================================================================
+struct MomentumArgs {
+  const float* div;
+  const float* sgs_u;
+  const float* sgs_v;
+  const float* sgs_w;
+  float* Ru;
+  float* Rv;
+  float* Rw;
+  int wmode;
+};
+
+// face fluxes of u, v and w through the faces (x: which 0, y: 1, z: 2) whose right/upper point
+// is box (lx, ly, lz).  Mass fluxes: advection.py:678-767 (u), :933-1024 (v), :1186-1281 (w) and
+// the vertical ones :561-676, :816-931, :1070-1184.
+__device__ __forceinline__ void momentum_face(const Box& bu, const Box& bv, const Box& bw, const Cols& c, const Idx& ix,
+                                              int which, int lx, int ly, int lz, int nz, float& fu, float& fv,
+                                              float& fw) {
+  fu = 0.f;
+  fv = 0.f;
+  fw = 0.f;
+  const float eps = kWepsMom;
+  const int k = ix.zl[lz];
+  if (which == 0) {
+    if (k >= 0 && k < nz) {
+      const float r = c.rho[k];
+      fu = wx(bu, lx, ly, lz, 0.5f * (bu[lz][ly][lx - 1] + bu[lz][ly][lx]) * r, eps);  // cell between u's
+      fv = wx(bv, lx, ly, lz, 0.5f * (r * bu[lz][ly - 1][lx] + r * bu[lz][ly][lx]), eps);  // corner
+    }
+    if (k >= 1 && k < nz) {  // w's lateral faces on interior face levels
+      const float m = 0.5f * (c.rho[k - 1] * bu[lz - 1][ly][lx] + c.rho[k] * bu[lz][ly][lx]);
+      fw = wx(bw, lx, ly, lz, m, eps);
+    }
+  } else if (which == 1) {
+    if (k >= 0 && k < nz) {
+      const float r = c.rho[k];
+      fu = wy(bu, lx, ly, lz, 0.5f * (r * bv[lz][ly][lx - 1] + r * bv[lz][ly][lx]), eps);  // corner
+      fv = wy(bv, lx, ly, lz, 0.5f * (bv[lz][ly - 1][lx] + bv[lz][ly][lx]) * r, eps);      // cell between v's
+    }
+    if (k >= 1 && k < nz) {
+      const float m = 0.5f * (c.rho[k - 1] * bv[lz - 1][ly][lx] + c.rho[k] * bv[lz][ly][lx]);
+      fw = wy(bw, lx, ly, lz, m, eps);
+    }
+  } else {
+    const int H = k;
+    if (H >= 1 && H < nz) {  // u and v columns: faces between cell levels, zero at the ends
+      const float rf = c.rho_face[H];
+      fu = wz(bu, lx, ly, lz, 0.5f * (rf * bw[lz][ly][lx - 1] + rf * bw[lz][ly][lx]), H, nz, eps);
+      fv = wz(bv, lx, ly, lz, 0.5f * (rf * bw[lz][ly - 1][lx] + rf * bw[lz][ly][lx]), H, nz, eps);
+    }
+    if (H >= 1 && H <= nz) {  // w column: its face H is the cell H-1
+      fw = wz(bw, lx, ly, lz, 0.5f * (bw[lz - 1][ly][lx] + bw[lz][ly][lx]) * c.rho[H - 1], H, nz + 1, eps);
+    }
+  }
+}
+
+// 67.6 KB of shared memory: above the 48 KB static limit, so it is carved from dynamic shared
+// memory (opted in once per process by init_weno_attributes).
+struct MomentumSmem {
+  Box bu, bv, bw;
+  FluxX xu, xv, xw;
+  FluxY yu, yv, yw;
+  FluxZ zu, zv, zw;
+  Idx ix;
+};
+
+__global__ void __launch_bounds__(NT) k_weno_momentum(Dims d, Phys ph, Cols c, State s, MomentumArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  MomentumSmem& S = *reinterpret_cast<MomentumSmem*>(smem_raw);
+  Box &bu = S.bu, &bv = S.bv, &bw = S.bw;
+  FluxX &xu = S.xu, &xv = S.xv, &xw = S.xw;
+  FluxY &yu = S.yu, &yv = S.yv, &yw = S.yw;
+  FluxZ &zu = S.zu, &zv = S.zv, &zw = S.zw;
+  Idx& ix = S.ix;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int plane = d.plane();
+  const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
+  const int tid = (tz * TY + ty) * TX + tx, warp = tid >> 5;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * TZ;
+  build_idx(ix, tid, i0, j0, k0, d);
+  __syncthreads();
+  {
+    Box* const boxes[3] = {&bu, &bv, &bw};
+    const float* const src[3] = {s.u, s.v, s.w};
+    const int* const zb[3] = {ix.zc, ix.zc, ix.zw};
+    stage<3>(boxes, src, zb, ix, warp, tx);
+  }
+  const int lx = tx + HALO, ly = ty + HALO, lz = tz + HALO;
+  const int k = k0 + tz;
+  const bool own = (i0 + tx < nx) && (j0 + ty < ny) && (k <= nz);
+  const bool cell = own && k < nz;  // u and v live on cell levels only
+  const int col = ix.x[lx], row = ix.y[ly];
+  const int id = k * plane + row + col;
+  float dc = 0.f, dxm = 0.f, dym = 0.f, dzm = 0.f, su = 0.f, sv = 0.f, sw = 0.f;
+  if (cell) {
+    dc = LD(a.div, id);
+    dxm = LD(a.div, k * plane + row + ix.x[lx - 1]);
+    dym = LD(a.div, k * plane + ix.y[ly - 1] + col);
+    if (a.sgs_u) {
+      su = LD(a.sgs_u, id);
+      sv = LD(a.sgs_v, id);
+    }
+  }
+  if (own && k >= 1 && k < nz) dzm = LD(a.div, id - plane);
+  if (own && a.sgs_w) sw = LD(a.sgs_w, id);
+  __syncthreads();
+  momentum_face(bu, bv, bw, c, ix, 0, lx, ly, lz, nz, xu[tz][ty][tx], xv[tz][ty][tx], xw[tz][ty][tx]);
+  momentum_face(bu, bv, bw, c, ix, 1, lx, ly, lz, nz, yu[tz][ty][tx], yv[tz][ty][tx], yw[tz][ty][tx]);
+  momentum_face(bu, bv, bw, c, ix, 2, lx, ly, lz, nz, zu[tz][ty][tx], zv[tz][ty][tx], zw[tz][ty][tx]);
+  if (warp < 4) {
+    momentum_face(bu, bv, bw, c, ix, 1, lx, TY + HALO, warp + HALO, nz, yu[warp][TY][tx], yv[warp][TY][tx],
+                  yw[warp][TY][tx]);
+  } else if (warp < 8) {
+    const int ey = warp - 4;
+    momentum_face(bu, bv, bw, c, ix, 2, lx, ey + HALO, TZ + HALO, nz, zu[TZ][ey][tx], zv[TZ][ey][tx], zw[TZ][ey][tx]);
+  } else if (warp == 8 && tx < TY * TZ) {
+    const int ey = tx % TY, ez = tx / TY;
+    momentum_face(bu, bv, bw, c, ix, 0, TX + HALO, ey + HALO, ez + HALO, nz, xu[ez][ey][TX], xv[ez][ey][TX],
+                  xw[ez][ey][TX]);
+  }
+  __syncthreads();
+  if (!own) return;
+  if (cell) {
+    const float r = c.rho[k];
+    const float cu = -((xu[tz][ty][tx + 1] - xu[tz][ty][tx]) * ph.rdx + (yu[tz][ty + 1][tx] - yu[tz][ty][tx]) * ph.rdy +
+                       (zu[tz + 1][ty][tx] - zu[tz][ty][tx]) * ph.rdz);
+    const float cv = -((xv[tz][ty][tx + 1] - xv[tz][ty][tx]) * ph.rdx + (yv[tz][ty + 1][tx] - yv[tz][ty][tx]) * ph.rdy +
+                       (zv[tz + 1][ty][tx] - zv[tz][ty][tx]) * ph.rdz);
+    float Ru = (cu + bu[lz][ly][lx] * (0.5f * (dxm + dc))) / r;
+    float Rv = (cv + bv[lz][ly][lx] * (0.5f * (dym + dc))) / r;
+    if (ph.cor_opt) {  // f v at u points, f u at v points (4-point averages)
+      const float fv = ph.f_cor * 0.25f * (bv[lz][ly][lx - 1] + bv[lz][ly + 1][lx - 1] + bv[lz][ly][lx] +
+                                           bv[lz][ly + 1][lx]);
+      float fu = 0.25f * (bu[lz][ly - 1][lx] + bu[lz][ly][lx] + bu[lz][ly - 1][lx + 1] + bu[lz][ly][lx + 1]);
+      fu = ph.cor_opt == 2 ? ph.f_cor * (fu - 1.0f) : ph.f_cor * fu;
+      Ru = Ru + fv;
+      Rv = Rv - fu;
+    }
+    if (a.sgs_u) {
+      Ru = Ru + su;
+      Rv = Rv + sv;
+    }
+    a.Ru[id] = Ru;
+    a.Rv[id] = Rv;
+  }
+  // w on face k
+  float adv = 0.f;
+  if (k >= 1 && k < nz) {
+    const float cw = -((xw[tz][ty][tx + 1] - xw[tz][ty][tx]) * ph.rdx + (yw[tz][ty + 1][tx] - yw[tz][ty][tx]) * ph.rdy +
+                       (zw[tz + 1][ty][tx] - zw[tz][ty][tx]) * ph.rdz);
+    adv = (cw + bw[lz][ly][lx] * (0.5f * (dzm + dc))) / (0.5f * (c.rho[k - 1] + c.rho[k]));
+  }
+  if (a.wmode == 1) {
+    a.Rw[id] = adv;
+    return;
+  }
+  auto b = [&](int kk) {
+    const int q = kk * plane + row + col;
+    return buoyancy_at(LD(s.T, q), LD(s.q, q), kk, c);
+  };
+  float b8w;
+  if (k == 0)
+    b8w = 1.875f * b(0) - 1.25f * b(1) + 0.375f * b(2);
+  else if (k == nz)
+    b8w = 1.875f * b(nz - 1) - 1.25f * b(nz - 2) + 0.375f * b(nz - 3);
+  else
+    b8w = 0.5f * (b(k - 1) + b(k));
+  if (a.wmode == 2) {
+    a.Rw[id] = b8w;
+    return;
+  }
+  float R = adv + b8w;
+  if (a.sgs_w) R = R + sw;
+  a.Rw[id] = R;
+}
+
+}  // namespace
+
+cudaError_t launch_adv_scalars(const Dims& d, const Phys& ph, const Cols& c, State in, const float* div,
+                               const float* T0, const float* q0, Sgs sgs, float dts, SlowOut out, cudaStream_t st) {
+  ScalarArgs a{div, T0, q0, sgs.T, sgs.q, out.T_next, out.q_next, out.dT, out.dq, dts};
+  dim3 g((d.nx + TX - 1) / TX, (d.ny + TY - 1) / TY, (d.nz + TZ - 1) / TZ);
+  k_weno_scalars<<<g, dim3(TX, TY, TZ), 0, st>>>(d, ph, c, in, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adv_momentum(const Dims& d, const Phys& ph, const Cols& c, State in, const float* div, Sgs sgs,
+                                float* Ru, float* Rv, float* Rw, int wmode, cudaStream_t st) {
+  MomentumArgs a{div, sgs.u, sgs.v, sgs.w, Ru, Rv, Rw, wmode};
+  dim3 g((d.nx + TX - 1) / TX, (d.ny + TY - 1) / TY, (d.nz + 1 + TZ - 1) / TZ);
+  k_weno_momentum<<<g, dim3(TX, TY, TZ), sizeof(MomentumSmem), st>>>(d, ph, c, in, a);
+  return cudaGetLastError();
+}
+
+cudaError_t init_weno_attributes() {
+  return cudaFuncSetAttribute(k_weno_momentum, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(MomentumSmem));
+}
+
+}  // namespace lexgb

@@ -206,13 +206,11 @@ struct Sgs {
 cudaError_t launch_div_trho(const Dims&, const Phys&, const Cols&, State in, float* div, float* trho, cudaStream_t);
 cudaError_t launch_adv_scalars(const Dims&, const Phys&, const Cols&, State in, const float* div, const float* T0,
                                const float* q0, Sgs sgs, float dts, SlowOut out, cudaStream_t);
-cudaError_t launch_adv_u(const Dims&, const Phys&, const Cols&, State in, const float* div, const float* sgs_u,
-                         float* Ru, cudaStream_t);
-cudaError_t launch_adv_v(const Dims&, const Phys&, const Cols&, State in, const float* div, const float* sgs_v,
-                         float* Rv, cudaStream_t);
-// mode 0: R_w = adv_w + b8w + sgs_w; mode 1: adv_w only; mode 2: b8w only
-cudaError_t launch_adv_w(const Dims&, const Phys&, const Cols&, State in, const float* div, const float* sgs_w,
-                         float* Rw, int mode, cudaStream_t);
+// once per process, before the first launch (opts the momentum kernel into > 48 KB of shared memory)
+cudaError_t init_weno_attributes();
+// u, v, w together; wmode 0: R_w = adv_w + b8w + sgs_w; 1: adv_w only; 2: b8w only
+cudaError_t launch_adv_momentum(const Dims&, const Phys&, const Cols&, State in, const float* div, Sgs sgs, float* Ru,
+                                float* Rv, float* Rw, int wmode, cudaStream_t);
 struct AcousticIn {
   const float *u, *v, *w, *p;       // sub-step start
   const float *Ru, *Rv, *Rw;        // slow tendencies
@@ -222,6 +220,10 @@ struct AcousticIn {
 struct AcousticOut { float *u, *v, *w, *p; };
 cudaError_t launch_acoustic(const Dims&, const Phys&, const Cols&, AcousticIn in, AcousticOut out, float dtau,
                             cudaStream_t);
+// two sub-steps in one launch (temporal blocking); in and out must not alias
+cudaError_t launch_acoustic_pair(const Dims&, const Phys&, const Cols&, AcousticIn in, AcousticOut out, float dtau,
+                                 cudaStream_t);
+cudaError_t init_acoustic_attributes();
 // diagnostics of the acoustic operators on one state
 cudaError_t launch_diag_pgf(const Dims&, const Phys&, const Cols&, const float* p, const float* trho, float* pu,
                             float* pv, float* pw, cudaStream_t);
