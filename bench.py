@@ -312,7 +312,7 @@ def run_lexgb(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="lexgb", choices=["lexgb", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
