@@ -19,6 +19,11 @@ namespace {
 constexpr int BX = 32, BY = 4, BZ = 2;
 #define LD(p, idx) __ldg((p) + (idx))
 
+// x points per thread of the vectorised sub-step kernel
+#ifndef ACOUSTIC_VEC
+#define ACOUSTIC_VEC 4
+#endif
+
 constexpr float kHalfCp = (float)(0.5 * kCp);
 constexpr float kRdCv = (float)(kRd / kCv);
 
@@ -93,87 +98,161 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_acoustic(Dims d, Phys ph, Cols c
   if (k == d.nz - 1) o.w[d.at(i, j, d.nz)] = 0.f;
 }
 
-// Vectorised sub-step: each thread owns 4 consecutive x points of one (j, k) row and moves
-// every field with 128-bit loads/stores (needs nx % 4 == 0).  Same arithmetic as k_acoustic.
-__device__ __forceinline__ float4 ld4(const float* __restrict__ p, int idx) {
-  return __ldg(reinterpret_cast<const float4*>(p + idx));
-}
-__device__ __forceinline__ float comp(const float4& v, int l) { return l == 0 ? v.x : (l == 1 ? v.y : (l == 2 ? v.z : v.w)); }
+// Vectorised sub-step: each thread owns V (4 or 2) consecutive x points of one (j, k) row and
+// moves every field with V-wide loads/stores (needs nx % V == 0).  Same arithmetic as k_acoustic.
+template <int V>
+struct VecT;
+template <>
+struct VecT<4> {
+  typedef float4 T;
+};
+template <>
+struct VecT<2> {
+  typedef float2 T;
+};
 
-__global__ void __launch_bounds__(256) k_acoustic4(Dims d, Phys ph, Cols c, AcousticIn a, AcousticOut o,
-                                                   float dtau) {
-  const int nq = d.nx >> 2;
+template <int V>
+__device__ __forceinline__ void ldv(const float* __restrict__ p, int idx, float (&o)[V]) {
+  typedef typename VecT<V>::T T;
+  const T t = __ldg(reinterpret_cast<const T*>(p + idx));
+  const float* f = reinterpret_cast<const float*>(&t);
+#pragma unroll
+  for (int l = 0; l < V; ++l) o[l] = f[l];
+}
+
+template <int V>
+__device__ __forceinline__ void stv(float* p, int idx, const float (&v)[V]) {
+  typedef typename VecT<V>::T T;
+  T t;
+  float* f = reinterpret_cast<float*>(&t);
+#pragma unroll
+  for (int l = 0; l < V; ++l) f[l] = v[l];
+  *reinterpret_cast<T*>(p + idx) = t;
+}
+
+template <int V>
+__device__ __forceinline__ void zero(float (&o)[V]) {
+#pragma unroll
+  for (int l = 0; l < V; ++l) o[l] = 0.f;
+}
+
+template <int V>
+__global__ void __launch_bounds__(256) k_acoustic_vec(Dims d, Phys ph, Cols c, AcousticIn a, AcousticOut o,
+                                                      float dtau) {
+  const int nq = d.nx / V;
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (q >= nq || j >= d.ny) return;
   const int nx = d.nx, nz = d.nz;
-  const int i0 = q << 2;
-  const int iw = wrap(i0 - 1, nx), ie = wrap(i0 + 4, nx);
+  const int i0 = q * V;
+  const int iw = wrap(i0 - 1, nx), ie = wrap(i0 + V, nx);
   const int jm = wrap(j - 1, d.ny), jp = wrap(j + 1, d.ny);
   const int r0 = (k * d.ny + j) * nx;
   const int rs = (k * d.ny + jm) * nx, rn = (k * d.ny + jp) * nx;
   const int rb = r0 - d.plane(), rt = r0 + d.plane();
   const bool has_b = k > 0, has_t = k + 1 < nz;
+  float P[V], TR[V], U[V], RU[V], Vv[V], RV[V], PS[V], TS[V], VN[V], RVN[V], PN[V], TN[V];
+  float W[V], RW[V], PB[V], TB[V], WT[V], RWT[V], PT[V], TT[V], S0[V], SS[V], SN[V], SB[V], ST[V];
   // centre row
-  const float4 P = ld4(a.p, r0 + i0), TR = ld4(a.trho, r0 + i0), U = ld4(a.u, r0 + i0), RU = ld4(a.Ru, r0 + i0);
+  ldv<V>(a.p, r0 + i0, P);
+  ldv<V>(a.trho, r0 + i0, TR);
+  ldv<V>(a.u, r0 + i0, U);
+  ldv<V>(a.Ru, r0 + i0, RU);
   const float pW = __ldg(a.p + r0 + iw), pE = __ldg(a.p + r0 + ie);
   const float tW = __ldg(a.trho + r0 + iw), tE = __ldg(a.trho + r0 + ie);
   const float uE = __ldg(a.u + r0 + ie), ruE = __ldg(a.Ru + r0 + ie);
   // south / north rows
-  const float4 V = ld4(a.v, r0 + i0), RV = ld4(a.Rv, r0 + i0);
-  const float4 PS = ld4(a.p, rs + i0), TS = ld4(a.trho, rs + i0);
-  const float4 VN = ld4(a.v, rn + i0), RVN = ld4(a.Rv, rn + i0);
-  const float4 PN = ld4(a.p, rn + i0), TN = ld4(a.trho, rn + i0);
+  ldv<V>(a.v, r0 + i0, Vv);
+  ldv<V>(a.Rv, r0 + i0, RV);
+  ldv<V>(a.p, rs + i0, PS);
+  ldv<V>(a.trho, rs + i0, TS);
+  ldv<V>(a.v, rn + i0, VN);
+  ldv<V>(a.Rv, rn + i0, RVN);
+  ldv<V>(a.p, rn + i0, PN);
+  ldv<V>(a.trho, rn + i0, TN);
   // bottom / top levels
-  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  const float4 W = has_b ? ld4(a.w, r0 + i0) : z4, RW = has_b ? ld4(a.Rw, r0 + i0) : z4;
-  const float4 PB = has_b ? ld4(a.p, rb + i0) : z4, TB = has_b ? ld4(a.trho, rb + i0) : z4;
-  const float4 WT = has_t ? ld4(a.w, rt + i0) : z4, RWT = has_t ? ld4(a.Rw, rt + i0) : z4;
-  const float4 PT = has_t ? ld4(a.p, rt + i0) : z4, TT = has_t ? ld4(a.trho, rt + i0) : z4;
+  if (has_b) {
+    ldv<V>(a.w, r0 + i0, W);
+    ldv<V>(a.Rw, r0 + i0, RW);
+    ldv<V>(a.p, rb + i0, PB);
+    ldv<V>(a.trho, rb + i0, TB);
+    ldv<V>(a.ps, rb + i0, SB);
+  } else {
+    zero<V>(W); zero<V>(RW); zero<V>(PB); zero<V>(TB); zero<V>(SB);
+  }
+  if (has_t) {
+    ldv<V>(a.w, rt + i0, WT);
+    ldv<V>(a.Rw, rt + i0, RWT);
+    ldv<V>(a.p, rt + i0, PT);
+    ldv<V>(a.trho, rt + i0, TT);
+    ldv<V>(a.ps, rt + i0, ST);
+  } else {
+    zero<V>(WT); zero<V>(RWT); zero<V>(PT); zero<V>(TT); zero<V>(ST);
+  }
   // pi'_s for advection_pi
-  const float4 S0 = ld4(a.ps, r0 + i0), SS = ld4(a.ps, rs + i0), SN = ld4(a.ps, rn + i0);
-  const float4 SB = has_b ? ld4(a.ps, rb + i0) : z4, ST = has_t ? ld4(a.ps, rt + i0) : z4;
+  ldv<V>(a.ps, r0 + i0, S0);
+  ldv<V>(a.ps, rs + i0, SS);
+  ldv<V>(a.ps, rn + i0, SN);
   const float sW = __ldg(a.ps + r0 + iw), sE = __ldg(a.ps + r0 + ie);
 
-  float un[5];
+  float un[V + 1];
   {
-    const float pc[6] = {pW, P.x, P.y, P.z, P.w, pE};
-    const float tc[6] = {tW, TR.x, TR.y, TR.z, TR.w, tE};
-    const float uc[5] = {U.x, U.y, U.z, U.w, uE};
-    const float rc[5] = {RU.x, RU.y, RU.z, RU.w, ruE};
+    float pc[V + 2], tc[V + 2], uc[V + 1], rc[V + 1];
+    pc[0] = pW;
+    tc[0] = tW;
+    pc[V + 1] = pE;
+    tc[V + 1] = tE;
+    uc[V] = uE;
+    rc[V] = ruE;
 #pragma unroll
-    for (int l = 0; l < 5; ++l) un[l] = uc[l] + (pgf(tc[l + 1], tc[l], pc[l + 1], pc[l], ph.rdx) + rc[l]) * dtau;
+    for (int l = 0; l < V; ++l) {
+      pc[l + 1] = P[l];
+      tc[l + 1] = TR[l];
+      uc[l] = U[l];
+      rc[l] = RU[l];
+    }
+#pragma unroll
+    for (int l = 0; l <= V; ++l) un[l] = uc[l] + (pgf(tc[l + 1], tc[l], pc[l + 1], pc[l], ph.rdx) + rc[l]) * dtau;
   }
-  const float sc[6] = {sW, S0.x, S0.y, S0.z, S0.w, sE};
+  float sc[V + 2];
+  sc[0] = sW;
+  sc[V + 1] = sE;
+#pragma unroll
+  for (int l = 0; l < V; ++l) sc[l + 1] = S0[l];
   const float rho = c.rho[k], rfb = c.rho_face[k], rft = c.rho_face[k + 1];
   const float dzb = c.dpi0dz[k], dzt = c.dpi0dz[k + 1], pi0 = c.pi0[k];
-  float outp[4], outv[4], outw[4];
+  float outp[V], outv[V], outw[V], outu[V];
 #pragma unroll
-  for (int l = 0; l < 4; ++l) {
-    const float p0 = comp(P, l), t0 = comp(TR, l);
-    const float vs = comp(V, l) + (pgf(t0, comp(TS, l), p0, comp(PS, l), ph.rdy) + comp(RV, l)) * dtau;
-    const float vn = comp(VN, l) + (pgf(comp(TN, l), t0, comp(PN, l), p0, ph.rdy) + comp(RVN, l)) * dtau;
-    const float wb = has_b ? comp(W, l) + (pgf(t0, comp(TB, l), p0, comp(PB, l), ph.rdz) + comp(RW, l)) * dtau : 0.f;
-    const float wt = has_t ? comp(WT, l) + (pgf(comp(TT, l), t0, comp(PT, l), p0, ph.rdz) + comp(RWT, l)) * dtau : 0.f;
+  for (int l = 0; l < V; ++l) {
+    const float p0 = P[l], t0 = TR[l];
+    const float vs = Vv[l] + (pgf(t0, TS[l], p0, PS[l], ph.rdy) + RV[l]) * dtau;
+    const float vn = VN[l] + (pgf(TN[l], t0, PN[l], p0, ph.rdy) + RVN[l]) * dtau;
+    const float wb = has_b ? W[l] + (pgf(t0, TB[l], p0, PB[l], ph.rdz) + RW[l]) * dtau : 0.f;
+    const float wt = has_t ? WT[l] + (pgf(TT[l], t0, PT[l], p0, ph.rdz) + RWT[l]) * dtau : 0.f;
     const float div = (un[l + 1] - un[l]) * ph.rdx + (vn - vs) * ph.rdy + (wt - wb) * ph.rdz;
     const float s0 = sc[l + 1];
     const float gxw = (s0 - sc[l]) * ph.rdx, gxe = (sc[l + 2] - s0) * ph.rdx;
-    const float gys = (s0 - comp(SS, l)) * ph.rdy, gyn = (comp(SN, l) - s0) * ph.rdy;
-    const float wzb = has_b ? wb * (dzb + (s0 - comp(SB, l)) * ph.rdz) : 0.f;
-    const float wzt = has_t ? wt * (dzt + (comp(ST, l) - s0) * ph.rdz) : 0.f;
+    const float gys = (s0 - SS[l]) * ph.rdy, gyn = (SN[l] - s0) * ph.rdy;
+    const float wzb = has_b ? wb * (dzb + (s0 - SB[l]) * ph.rdz) : 0.f;
+    const float wzt = has_t ? wt * (dzt + (ST[l] - s0) * ph.rdz) : 0.f;
     const float ap = -(0.5f * (un[l + 1] * gxe + un[l] * gxw) + 0.5f * (vn * gyn + vs * gys) +
                        (0.5f * wzb * rfb + 0.5f * wzt * rft) / rho);
     const float dpdt = -kRdCv * ((pi0 + s0) * div) + ap;
     outp[l] = p0 + (kDivDamp * dpdt) * dtau;
     outv[l] = vs;
     outw[l] = wb;
+    outu[l] = un[l];
   }
-  *reinterpret_cast<float4*>(o.p + r0 + i0) = make_float4(outp[0], outp[1], outp[2], outp[3]);
-  *reinterpret_cast<float4*>(o.u + r0 + i0) = make_float4(un[0], un[1], un[2], un[3]);
-  *reinterpret_cast<float4*>(o.v + r0 + i0) = make_float4(outv[0], outv[1], outv[2], outv[3]);
-  *reinterpret_cast<float4*>(o.w + r0 + i0) = make_float4(outw[0], outw[1], outw[2], outw[3]);
-  if (k == nz - 1) *reinterpret_cast<float4*>(o.w + rt + i0) = z4;
+  stv<V>(o.p, r0 + i0, outp);
+  stv<V>(o.u, r0 + i0, outu);
+  stv<V>(o.v, r0 + i0, outv);
+  stv<V>(o.w, r0 + i0, outw);
+  if (k == nz - 1) {
+    float z[V];
+    zero<V>(z);
+    stv<V>(o.w, rt + i0, z);
+  }
 }
 
 // ================================================================================================
@@ -476,11 +555,12 @@ __global__ void k_diag_advpi(Dims d, Phys ph, Cols c, const float* __restrict__ 
 
 cudaError_t launch_acoustic(const Dims& d, const Phys& ph, const Cols& c, AcousticIn in, AcousticOut out, float dtau,
                             cudaStream_t st) {
-  if (d.nx % 4 == 0) {
-    const int nq = d.nx / 4;
-    dim3 b(16, 16, 1);
+  constexpr int VW = ACOUSTIC_VEC;
+  if (d.nx % VW == 0) {
+    const int nq = d.nx / VW;
+    dim3 b(VW == 4 ? 16 : 32, VW == 4 ? 16 : 8, 1);
     dim3 g((nq + b.x - 1) / b.x, (d.ny + b.y - 1) / b.y, d.nz);
-    k_acoustic4<<<g, b, 0, st>>>(d, ph, c, in, out, dtau);
+    k_acoustic_vec<VW><<<g, b, 0, st>>>(d, ph, c, in, out, dtau);
     return cudaGetLastError();
   }
   dim3 g((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, (d.nz + BZ - 1) / BZ);
