@@ -9,11 +9,13 @@
 // mass fluxes are averages of the three winds, all staged in shared memory).
 //
 // A block owns a 32 x 4 x 4 box of points, one thread per point.  It stages each field on the
-// box plus a 3-cell halo in shared memory (periodic in x and y, clamped in z), evaluates every x,
-// y and z face flux of the box exactly once - each thread its point's west, south and bottom
-// faces, whole warps the box's north, top and east edge faces - and forms each point's tendency
-// from its six face fluxes.  The upwind stencil is selected from the sign of the mass flux
-// before the reconstruction.  Global indices of the halo coordinates are tabulated per block.
+// box plus halo in shared memory (periodic in x and y, clamped in z; x rows are widened to 40
+// floats starting at i0-4 so that rows move as aligned float4s when nx % 4 == 0), evaluates
+// every x, y and z face flux of the box exactly once - each thread its point's west, south and
+// bottom faces, whole warps the box's north, top and east edge faces - and forms each point's
+// tendency from its six face fluxes.  Everything a thread's own faces and its point need from
+// global memory is loaded before the first barrier; the upwind stencil is selected from the
+// sign of the mass flux before the reconstruction.
 //
 // Outputs (one_step_integration.py:258-296):
 //   theta, qv : phi_next = phi^0 + dt_s * adv (+ dt_s * sgs); optional record of adv (+ sgs)
@@ -28,9 +30,10 @@ namespace lexgb {
 
 namespace {
 
-constexpr int TX = 32, TY = 4, TZ = 4, HALO = 3;
+constexpr int TX = 32, TY = 4, TZ = 4, HALO = 3, HX = 4;
 constexpr int NT = TX * TY * TZ;
-constexpr int BX3 = TX + 2 * HALO, BY3 = TY + 2 * HALO, BZ3 = TZ + 2 * HALO;
+constexpr int BX3 = TX + 2 * HX, BY3 = TY + 2 * HALO, BZ3 = TZ + 2 * HALO;  // 40 x 10 x 10
+constexpr int NWARP = NT / 32;
 
 typedef float Box[BZ3][BY3][BX3];
 typedef float FluxX[TZ][TY][TX + 1];
@@ -44,65 +47,91 @@ __device__ __forceinline__ int pmod(int i, int n) {
 
 #define LD(p, idx) __ldg((p) + (idx))
 
-// global index tables of the box's halo coordinates
+// global index tables of the box's halo coordinates (box column lx <-> x = i0 - 4 + lx,
+// row ly <-> y = j0 - 3 + ly, layer lz <-> level k0 - 3 + lz)
 struct Idx {
-  int x[BX3];   // x index of box column lx
-  int y[BY3];   // y index of box row ly, times nx
-  int zc[BZ3];  // cell level of box layer lz clamped to 0..nz-1, times nx*ny
+  int x[BX3];   // wrapped x
+  int y[BY3];   // wrapped y, times nx
+  int zc[BZ3];  // cell level clamped to 0..nz-1, times nx*ny
   int zw[BZ3];  // face level clamped to 0..nz, times nx*ny
-  int zl[BZ3];  // unclamped level k0 - 3 + lz
 };
 
 __device__ __forceinline__ void build_idx(Idx& ix, int tid, int i0, int j0, int k0, const Dims& d) {
   if (tid < BX3) {
-    ix.x[tid] = pmod(i0 - HALO + tid, d.nx);
+    ix.x[tid] = pmod(i0 - HX + tid, d.nx);
   } else if (tid < BX3 + BY3) {
     ix.y[tid - BX3] = pmod(j0 - HALO + (tid - BX3), d.ny) * d.nx;
   } else if (tid < BX3 + BY3 + BZ3) {
     const int lz = tid - BX3 - BY3;
     const int k = k0 - HALO + lz;
-    ix.zl[lz] = k;
     ix.zc[lz] = clampi(k, 0, d.nz - 1) * d.plane();
     ix.zw[lz] = clampi(k, 0, d.nz) * d.plane();
   }
 }
 
-// Warp-per-row staging of NF fields on their boxes: warp w loads box rows w, w + 16, ... of every
-// field (lanes cover x; lanes 0..5 also the last 6 columns).  All loads are issued before any
-// shared-memory store, so a block pays one memory latency for its whole staging.
-constexpr int NWARP = NT / 32;
+// Staging of NF fields on their boxes with all loads in flight before any shared store.
+// vec4: rows move as 10 aligned float4s (nx % 4 == 0, so a 4-group never straddles the periodic
+// seam); otherwise warp-per-row scalar loads.
 constexpr int ROWS = BY3 * BZ3;
+constexpr int NQ4 = ROWS * (BX3 / 4);
+constexpr int IT4 = (NQ4 + NT - 1) / NT;
 constexpr int RPW = (ROWS + NWARP - 1) / NWARP;
 
 template <int NF>
 __device__ __forceinline__ void stage(Box* const (&b)[NF], const float* const (&f)[NF], const int* const (&zbase)[NF],
-                                      const Idx& ix, int warp, int lane) {
-  const int xa = ix.x[lane];
-  const bool tail = lane < BX3 - 32;
-  const int xb = tail ? ix.x[32 + lane] : 0;
-  float va[NF][RPW], vb[NF][RPW];
+                                      const Idx& ix, int tid, bool vec4) {
+  if (vec4) {
+    float4 v[NF][IT4];
 #pragma unroll
-  for (int q = 0; q < RPW; ++q) {
-    const int r = warp + q * NWARP;
-    if (r < ROWS) {
-      const int lz = r / BY3, ly = r - lz * BY3;
+    for (int q = 0; q < IT4; ++q) {
+      const int t = tid + q * NT;
+      if (t < NQ4) {
+        const int r = t / (BX3 / 4), c4 = t - r * (BX3 / 4);
+        const int lz = r / BY3, ly = r - lz * BY3;
 #pragma unroll
-      for (int n = 0; n < NF; ++n) {
-        const int base = zbase[n][lz] + ix.y[ly];
-        va[n][q] = LD(f[n], base + xa);
-        vb[n][q] = tail ? LD(f[n], base + xb) : 0.f;
+        for (int n = 0; n < NF; ++n)
+          v[n][q] = __ldg(reinterpret_cast<const float4*>(f[n] + zbase[n][lz] + ix.y[ly] + ix.x[4 * c4]));
       }
     }
-  }
 #pragma unroll
-  for (int q = 0; q < RPW; ++q) {
-    const int r = warp + q * NWARP;
-    if (r < ROWS) {
-      const int lz = r / BY3, ly = r - lz * BY3;
+    for (int q = 0; q < IT4; ++q) {
+      const int t = tid + q * NT;
+      if (t < NQ4) {
+        const int r = t / (BX3 / 4), c4 = t - r * (BX3 / 4);
+        const int lz = r / BY3, ly = r - lz * BY3;
 #pragma unroll
-      for (int n = 0; n < NF; ++n) {
-        (*b[n])[lz][ly][lane] = va[n][q];
-        if (tail) (*b[n])[lz][ly][32 + lane] = vb[n][q];
+        for (int n = 0; n < NF; ++n) *reinterpret_cast<float4*>(&(*b[n])[lz][ly][4 * c4]) = v[n][q];
+      }
+    }
+  } else {
+    const int lane = tid & 31, warp = tid >> 5;
+    const int xa = ix.x[lane];
+    const bool tail = lane < BX3 - 32;
+    const int xb = tail ? ix.x[32 + lane] : 0;
+    float va[NF][RPW], vb[NF][RPW];
+#pragma unroll
+    for (int q = 0; q < RPW; ++q) {
+      const int r = warp + q * NWARP;
+      if (r < ROWS) {
+        const int lz = r / BY3, ly = r - lz * BY3;
+#pragma unroll
+        for (int n = 0; n < NF; ++n) {
+          const int base = zbase[n][lz] + ix.y[ly];
+          va[n][q] = LD(f[n], base + xa);
+          vb[n][q] = tail ? LD(f[n], base + xb) : 0.f;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < RPW; ++q) {
+      const int r = warp + q * NWARP;
+      if (r < ROWS) {
+        const int lz = r / BY3, ly = r - lz * BY3;
+#pragma unroll
+        for (int n = 0; n < NF; ++n) {
+          (*b[n])[lz][ly][lane] = va[n][q];
+          if (tail) (*b[n])[lz][ly][32 + lane] = vb[n][q];
+        }
       }
     }
   }
@@ -136,8 +165,8 @@ __device__ __forceinline__ float vflux6(float m, float sm3, float sm2, float sm1
   return m * r;
 }
 
-// WENO face fluxes of a staged field: box coordinates (lx, ly, lz) of the point right of / above
-// the face
+// WENO face fluxes of a staged field at box coordinates (lx, ly, lz) of the point right of /
+// above the face
 __device__ __forceinline__ float wx(const Box& b, int lx, int ly, int lz, float m, float eps) {
   return weno_flux(m, b[lz][ly][lx - 3], b[lz][ly][lx - 2], b[lz][ly][lx - 1], b[lz][ly][lx], b[lz][ly][lx + 1],
                    b[lz][ly][lx + 2], eps);
@@ -149,6 +178,26 @@ __device__ __forceinline__ float wy(const Box& b, int lx, int ly, int lz, float 
 __device__ __forceinline__ float wz(const Box& b, int lx, int ly, int lz, float m, int H, int n, float eps) {
   return vflux6(m, b[lz - 3][ly][lx], b[lz - 2][ly][lx], b[lz - 1][ly][lx], b[lz][ly][lx], b[lz + 1][ly][lx],
                 b[lz + 2][ly][lx], H, n, eps);
+}
+
+// Edge faces: warps 0-3 the north faces of layer `warp`, warps 4-7 the top faces of row warp-4,
+// warp 8 (16 lanes) the east faces of (row, layer) = (lane % TY, lane / TY).
+struct EdgeFace {
+  int which;       // -1 none, 0 x, 1 y, 2 z
+  int lx, ly, lz;  // box coordinates of the point right of / above the face
+  int fi, fj, fk;  // slot in the flux arrays
+};
+
+__device__ __forceinline__ EdgeFace edge_face(int warp, int lane) {
+  EdgeFace e{-1, 0, 0, 0, 0, 0, 0};
+  if (warp < 4) {
+    e = EdgeFace{1, lane + HX, TY + HALO, warp + HALO, lane, TY, warp};
+  } else if (warp < 8) {
+    e = EdgeFace{2, lane + HX, warp - 4 + HALO, TZ + HALO, lane, warp - 4, TZ};
+  } else if (warp == 8 && lane < TY * TZ) {
+    e = EdgeFace{0, TX + HX, lane % TY + HALO, lane / TY + HALO, TX, lane % TY, lane / TY};
+  }
+  return e;
 }
 
 // ================================================================================================
@@ -167,56 +216,51 @@ struct ScalarArgs {
   float dts;
 };
 
-// the three face fluxes (x, y, z) of both scalars through the faces whose right/upper point is
-// box (lx, ly, lz); `which` selects x (0), y (1) or z (2)
-__device__ __forceinline__ void scalar_face(const Box& bT, const Box& bQ, const Cols& c, const State& s, const Idx& ix,
-                                            int which, int lx, int ly, int lz, int nz, float& fT, float& fQ) {
-  fT = 0.f;
-  fQ = 0.f;
-  const int k = ix.zl[lz];
-  if (which < 2) {
-    if (k < 0 || k >= nz) return;
-    const int g = ix.zc[lz] + ix.y[ly] + ix.x[lx];
-    if (which == 0) {
-      const float m = c.rho[k] * LD(s.u, g);
-      fT = wx(bT, lx, ly, lz, m, kWepsTheta);
-      fQ = wx(bQ, lx, ly, lz, m, kWepsQv);
-    } else {
-      const float m = c.rho[k] * LD(s.v, g);
-      fT = wy(bT, lx, ly, lz, m, kWepsTheta);
-      fQ = wy(bQ, lx, ly, lz, m, kWepsQv);
-    }
-  } else {
-    const int H = k;  // bottom face of level k; zero on the surface (sfc flux 0) and the lid
-    if (H < 1 || H >= nz) return;
-    const float m = c.rho_face[H] * LD(s.w, ix.zw[lz] + ix.y[ly] + ix.x[lx]);
-    fT = wz(bT, lx, ly, lz, m, H, nz, kWepsTheta);
-    fQ = wz(bQ, lx, ly, lz, m, H, nz, kWepsQv);
-  }
-}
-
 __global__ void __launch_bounds__(NT) k_weno_scalars(Dims d, Phys ph, Cols c, State s, ScalarArgs a) {
-  __shared__ Box bT, bQ;
+  __shared__ __align__(16) Box bT;
+  __shared__ __align__(16) Box bQ;
   __shared__ FluxX xT, xQ;
   __shared__ FluxY yT, yQ;
   __shared__ FluxZ zT, zQ;
   __shared__ Idx ix;
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
   const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
   const int tid = (tz * TY + ty) * TX + tx, warp = tid >> 5;
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * TZ;
   build_idx(ix, tid, i0, j0, k0, d);
   __syncthreads();
+  // ---- every global load of the block
   {
     Box* const boxes[2] = {&bT, &bQ};
     const float* const src[2] = {s.T, s.q};
     const int* const zb[2] = {ix.zc, ix.zc};
-    stage<2>(boxes, src, zb, ix, warp, tx);
+    stage<2>(boxes, src, zb, ix, tid, (nx & 3) == 0);
   }
-  const int lx = tx + HALO, ly = ty + HALO, lz = tz + HALO;
+  const int lx = tx + HX, ly = ty + HALO, lz = tz + HALO;
   const int k = k0 + tz;
-  const bool own = (i0 + tx < nx) && (j0 + ty < ny) && (k < nz);
-  const int id = k * d.plane() + ix.y[ly] + ix.x[lx];
+  const bool inlev = k < nz;
+  const bool own = (i0 + tx < nx) && (j0 + ty < ny) && inlev;
+  const int id = (inlev ? k : 0) * plane + ix.y[ly] + ix.x[lx];
+  // own faces: west (u of the own point), south (v), bottom (w at face k)
+  float mx = 0.f, my = 0.f, mz = 0.f;
+  if (inlev) {
+    const float r = c.rho[k];
+    mx = r * LD(s.u, id);
+    my = r * LD(s.v, id);
+    if (k >= 1) mz = c.rho_face[k] * LD(s.w, id);
+  }
+  const EdgeFace e = edge_face(warp, tx);
+  float me = 0.f;
+  int He = 0;
+  if (e.which >= 0) {
+    const int ke = k0 - HALO + e.lz;
+    if (e.which == 0 && ke < nz) me = c.rho[ke] * LD(s.u, ke * plane + ix.y[e.ly] + ix.x[e.lx]);
+    if (e.which == 1 && ke < nz) me = c.rho[ke] * LD(s.v, ke * plane + ix.y[e.ly] + ix.x[e.lx]);
+    if (e.which == 2) {
+      He = ke;
+      if (He >= 1 && He < nz) me = c.rho_face[He] * LD(s.w, He * plane + ix.y[e.ly] + ix.x[e.lx]);
+    }
+  }
   float dv = 0.f, sT = 0.f, sQ = 0.f, T0 = 0.f, Q0 = 0.f;
   if (own) {
     dv = LD(a.div, id);
@@ -228,17 +272,25 @@ __global__ void __launch_bounds__(NT) k_weno_scalars(Dims d, Phys ph, Cols c, St
     Q0 = a.q0[id];
   }
   __syncthreads();
-  scalar_face(bT, bQ, c, s, ix, 0, lx, ly, lz, nz, xT[tz][ty][tx], xQ[tz][ty][tx]);
-  scalar_face(bT, bQ, c, s, ix, 1, lx, ly, lz, nz, yT[tz][ty][tx], yQ[tz][ty][tx]);
-  scalar_face(bT, bQ, c, s, ix, 2, lx, ly, lz, nz, zT[tz][ty][tx], zQ[tz][ty][tx]);
-  if (warp < 4) {  // north faces of layer `warp`
-    scalar_face(bT, bQ, c, s, ix, 1, lx, TY + HALO, warp + HALO, nz, yT[warp][TY][tx], yQ[warp][TY][tx]);
-  } else if (warp < 8) {  // top faces of row warp-4
-    const int ey = warp - 4;
-    scalar_face(bT, bQ, c, s, ix, 2, lx, ey + HALO, TZ + HALO, nz, zT[TZ][ey][tx], zQ[TZ][ey][tx]);
-  } else if (warp == 8 && tx < TY * TZ) {  // east faces
-    const int ey = tx % TY, ez = tx / TY;
-    scalar_face(bT, bQ, c, s, ix, 0, TX + HALO, ey + HALO, ez + HALO, nz, xT[ez][ey][TX], xQ[ez][ey][TX]);
+  // ---- face fluxes
+  const float eT = kWepsTheta, eQ = kWepsQv;
+  if (inlev) {
+    xT[tz][ty][tx] = wx(bT, lx, ly, lz, mx, eT);
+    xQ[tz][ty][tx] = wx(bQ, lx, ly, lz, mx, eQ);
+    yT[tz][ty][tx] = wy(bT, lx, ly, lz, my, eT);
+    yQ[tz][ty][tx] = wy(bQ, lx, ly, lz, my, eQ);
+  }
+  zT[tz][ty][tx] = wz(bT, lx, ly, lz, mz, k, nz, eT);  // zero outside 1..nz-1 (surface flux 0, lid)
+  zQ[tz][ty][tx] = wz(bQ, lx, ly, lz, mz, k, nz, eQ);
+  if (e.which == 0) {
+    xT[e.fk][e.fj][e.fi] = wx(bT, e.lx, e.ly, e.lz, me, eT);
+    xQ[e.fk][e.fj][e.fi] = wx(bQ, e.lx, e.ly, e.lz, me, eQ);
+  } else if (e.which == 1) {
+    yT[e.fk][e.fj][e.fi] = wy(bT, e.lx, e.ly, e.lz, me, eT);
+    yQ[e.fk][e.fj][e.fi] = wy(bQ, e.lx, e.ly, e.lz, me, eQ);
+  } else if (e.which == 2) {
+    zT[e.fk][e.fj][e.fi] = wz(bT, e.lx, e.ly, e.lz, me, He, nz, eT);
+    zQ[e.fk][e.fj][e.fi] = wz(bQ, e.lx, e.ly, e.lz, me, He, nz, eQ);
   }
   __syncthreads();
   if (!own) return;
@@ -276,54 +328,68 @@ struct MomentumArgs {
   int wmode;
 };
 
+// Column values a face at level k needs (loaded before the reconstruction work).
+struct LevelCols {
+  float r, rm, rf;  // rho0(k), rho0(k-1), rho0 on face k
+};
+
+__device__ __forceinline__ LevelCols level_cols(const Cols& c, int k, int nz) {
+  LevelCols l{0.f, 0.f, 0.f};
+  if (k >= 0 && k < nz) l.r = c.rho[k];
+  if (k >= 1 && k <= nz) l.rm = c.rho[k - 1];
+  if (k >= 0 && k <= nz) l.rf = c.rho_face[k];
+  return l;
+}
+
 // face fluxes of u, v and w through the faces (x: which 0, y: 1, z: 2) whose right/upper point
-// is box (lx, ly, lz).  Mass fluxes: advection.py:678-767 (u), :933-1024 (v), :1186-1281 (w) and
-// the vertical ones :561-676, :816-931, :1070-1184.
-__device__ __forceinline__ void momentum_face(const Box& bu, const Box& bv, const Box& bw, const Cols& c, const Idx& ix,
-                                              int which, int lx, int ly, int lz, int nz, float& fu, float& fv,
+// is box (lx, ly, lz) at level k.  Mass fluxes: advection.py:678-767 (u), :933-1024 (v),
+// :1186-1281 (w) and the vertical ones :561-676, :816-931, :1070-1184.
+__device__ __forceinline__ void momentum_face(const Box& bu, const Box& bv, const Box& bw, int which, int lx, int ly,
+                                              int lz, int k, const LevelCols& L, int nz, float& fu, float& fv,
                                               float& fw) {
   fu = 0.f;
   fv = 0.f;
   fw = 0.f;
   const float eps = kWepsMom;
-  const int k = ix.zl[lz];
   if (which == 0) {
     if (k >= 0 && k < nz) {
-      const float r = c.rho[k];
+      const float r = L.r;
       fu = wx(bu, lx, ly, lz, 0.5f * (bu[lz][ly][lx - 1] + bu[lz][ly][lx]) * r, eps);  // cell between u's
       fv = wx(bv, lx, ly, lz, 0.5f * (r * bu[lz][ly - 1][lx] + r * bu[lz][ly][lx]), eps);  // corner
     }
     if (k >= 1 && k < nz) {  // w's lateral faces on interior face levels
-      const float m = 0.5f * (c.rho[k - 1] * bu[lz - 1][ly][lx] + c.rho[k] * bu[lz][ly][lx]);
+      const float m = 0.5f * (L.rm * bu[lz - 1][ly][lx] + L.r * bu[lz][ly][lx]);
       fw = wx(bw, lx, ly, lz, m, eps);
     }
   } else if (which == 1) {
     if (k >= 0 && k < nz) {
-      const float r = c.rho[k];
+      const float r = L.r;
       fu = wy(bu, lx, ly, lz, 0.5f * (r * bv[lz][ly][lx - 1] + r * bv[lz][ly][lx]), eps);  // corner
       fv = wy(bv, lx, ly, lz, 0.5f * (bv[lz][ly - 1][lx] + bv[lz][ly][lx]) * r, eps);      // cell between v's
     }
     if (k >= 1 && k < nz) {
-      const float m = 0.5f * (c.rho[k - 1] * bv[lz - 1][ly][lx] + c.rho[k] * bv[lz][ly][lx]);
+      const float m = 0.5f * (L.rm * bv[lz - 1][ly][lx] + L.r * bv[lz][ly][lx]);
       fw = wy(bw, lx, ly, lz, m, eps);
     }
   } else {
     const int H = k;
     if (H >= 1 && H < nz) {  // u and v columns: faces between cell levels, zero at the ends
-      const float rf = c.rho_face[H];
+      const float rf = L.rf;
       fu = wz(bu, lx, ly, lz, 0.5f * (rf * bw[lz][ly][lx - 1] + rf * bw[lz][ly][lx]), H, nz, eps);
       fv = wz(bv, lx, ly, lz, 0.5f * (rf * bw[lz][ly - 1][lx] + rf * bw[lz][ly][lx]), H, nz, eps);
     }
     if (H >= 1 && H <= nz) {  // w column: its face H is the cell H-1
-      fw = wz(bw, lx, ly, lz, 0.5f * (bw[lz - 1][ly][lx] + bw[lz][ly][lx]) * c.rho[H - 1], H, nz + 1, eps);
+      fw = wz(bw, lx, ly, lz, 0.5f * (bw[lz - 1][ly][lx] + bw[lz][ly][lx]) * L.rm, H, nz + 1, eps);
     }
   }
 }
 
-// 67.6 KB of shared memory: above the 48 KB static limit, so it is carved from dynamic shared
+// 70 KB of shared memory: above the 48 KB static limit, so it is carved from dynamic shared
 // memory (opted in once per process by init_weno_attributes).
 struct MomentumSmem {
-  Box bu, bv, bw;
+  __align__(16) Box bu;
+  __align__(16) Box bv;
+  __align__(16) Box bw;
   FluxX xu, xv, xw;
   FluxY yu, yv, yw;
   FluxZ zu, zv, zw;
@@ -334,9 +400,6 @@ __global__ void __launch_bounds__(NT) k_weno_momentum(Dims d, Phys ph, Cols c, S
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MomentumSmem& S = *reinterpret_cast<MomentumSmem*>(smem_raw);
   Box &bu = S.bu, &bv = S.bv, &bw = S.bw;
-  FluxX &xu = S.xu, &xv = S.xv, &xw = S.xw;
-  FluxY &yu = S.yu, &yv = S.yv, &yw = S.yw;
-  FluxZ &zu = S.zu, &zv = S.zv, &zw = S.zw;
   Idx& ix = S.ix;
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int plane = d.plane();
@@ -349,14 +412,18 @@ __global__ void __launch_bounds__(NT) k_weno_momentum(Dims d, Phys ph, Cols c, S
     Box* const boxes[3] = {&bu, &bv, &bw};
     const float* const src[3] = {s.u, s.v, s.w};
     const int* const zb[3] = {ix.zc, ix.zc, ix.zw};
-    stage<3>(boxes, src, zb, ix, warp, tx);
+    stage<3>(boxes, src, zb, ix, tid, (nx & 3) == 0);
   }
-  const int lx = tx + HALO, ly = ty + HALO, lz = tz + HALO;
+  const int lx = tx + HX, ly = ty + HALO, lz = tz + HALO;
   const int k = k0 + tz;
   const bool own = (i0 + tx < nx) && (j0 + ty < ny) && (k <= nz);
   const bool cell = own && k < nz;  // u and v live on cell levels only
   const int col = ix.x[lx], row = ix.y[ly];
-  const int id = k * plane + row + col;
+  const int id = (k <= nz ? k : 0) * plane + row + col;
+  const LevelCols Lown = level_cols(c, k, nz);
+  const EdgeFace e = edge_face(warp, tx);
+  const int ke = k0 - HALO + e.lz;
+  const LevelCols Ledge = level_cols(c, ke, nz);
   float dc = 0.f, dxm = 0.f, dym = 0.f, dzm = 0.f, su = 0.f, sv = 0.f, sw = 0.f;
   if (cell) {
     dc = LD(a.div, id);
@@ -370,28 +437,29 @@ __global__ void __launch_bounds__(NT) k_weno_momentum(Dims d, Phys ph, Cols c, S
   if (own && k >= 1 && k < nz) dzm = LD(a.div, id - plane);
   if (own && a.sgs_w) sw = LD(a.sgs_w, id);
   __syncthreads();
-  momentum_face(bu, bv, bw, c, ix, 0, lx, ly, lz, nz, xu[tz][ty][tx], xv[tz][ty][tx], xw[tz][ty][tx]);
-  momentum_face(bu, bv, bw, c, ix, 1, lx, ly, lz, nz, yu[tz][ty][tx], yv[tz][ty][tx], yw[tz][ty][tx]);
-  momentum_face(bu, bv, bw, c, ix, 2, lx, ly, lz, nz, zu[tz][ty][tx], zv[tz][ty][tx], zw[tz][ty][tx]);
-  if (warp < 4) {
-    momentum_face(bu, bv, bw, c, ix, 1, lx, TY + HALO, warp + HALO, nz, yu[warp][TY][tx], yv[warp][TY][tx],
-                  yw[warp][TY][tx]);
-  } else if (warp < 8) {
-    const int ey = warp - 4;
-    momentum_face(bu, bv, bw, c, ix, 2, lx, ey + HALO, TZ + HALO, nz, zu[TZ][ey][tx], zv[TZ][ey][tx], zw[TZ][ey][tx]);
-  } else if (warp == 8 && tx < TY * TZ) {
-    const int ey = tx % TY, ez = tx / TY;
-    momentum_face(bu, bv, bw, c, ix, 0, TX + HALO, ey + HALO, ez + HALO, nz, xu[ez][ey][TX], xv[ez][ey][TX],
-                  xw[ez][ey][TX]);
+  momentum_face(bu, bv, bw, 0, lx, ly, lz, k, Lown, nz, S.xu[tz][ty][tx], S.xv[tz][ty][tx], S.xw[tz][ty][tx]);
+  momentum_face(bu, bv, bw, 1, lx, ly, lz, k, Lown, nz, S.yu[tz][ty][tx], S.yv[tz][ty][tx], S.yw[tz][ty][tx]);
+  momentum_face(bu, bv, bw, 2, lx, ly, lz, k, Lown, nz, S.zu[tz][ty][tx], S.zv[tz][ty][tx], S.zw[tz][ty][tx]);
+  if (e.which == 0) {
+    momentum_face(bu, bv, bw, 0, e.lx, e.ly, e.lz, ke, Ledge, nz, S.xu[e.fk][e.fj][e.fi], S.xv[e.fk][e.fj][e.fi],
+                  S.xw[e.fk][e.fj][e.fi]);
+  } else if (e.which == 1) {
+    momentum_face(bu, bv, bw, 1, e.lx, e.ly, e.lz, ke, Ledge, nz, S.yu[e.fk][e.fj][e.fi], S.yv[e.fk][e.fj][e.fi],
+                  S.yw[e.fk][e.fj][e.fi]);
+  } else if (e.which == 2) {
+    momentum_face(bu, bv, bw, 2, e.lx, e.ly, e.lz, ke, Ledge, nz, S.zu[e.fk][e.fj][e.fi], S.zv[e.fk][e.fj][e.fi],
+                  S.zw[e.fk][e.fj][e.fi]);
   }
   __syncthreads();
   if (!own) return;
   if (cell) {
-    const float r = c.rho[k];
-    const float cu = -((xu[tz][ty][tx + 1] - xu[tz][ty][tx]) * ph.rdx + (yu[tz][ty + 1][tx] - yu[tz][ty][tx]) * ph.rdy +
-                       (zu[tz + 1][ty][tx] - zu[tz][ty][tx]) * ph.rdz);
-    const float cv = -((xv[tz][ty][tx + 1] - xv[tz][ty][tx]) * ph.rdx + (yv[tz][ty + 1][tx] - yv[tz][ty][tx]) * ph.rdy +
-                       (zv[tz + 1][ty][tx] - zv[tz][ty][tx]) * ph.rdz);
+    const float r = Lown.r;
+    const float cu = -((S.xu[tz][ty][tx + 1] - S.xu[tz][ty][tx]) * ph.rdx +
+                       (S.yu[tz][ty + 1][tx] - S.yu[tz][ty][tx]) * ph.rdy +
+                       (S.zu[tz + 1][ty][tx] - S.zu[tz][ty][tx]) * ph.rdz);
+    const float cv = -((S.xv[tz][ty][tx + 1] - S.xv[tz][ty][tx]) * ph.rdx +
+                       (S.yv[tz][ty + 1][tx] - S.yv[tz][ty][tx]) * ph.rdy +
+                       (S.zv[tz + 1][ty][tx] - S.zv[tz][ty][tx]) * ph.rdz);
     float Ru = (cu + bu[lz][ly][lx] * (0.5f * (dxm + dc))) / r;
     float Rv = (cv + bv[lz][ly][lx] * (0.5f * (dym + dc))) / r;
     if (ph.cor_opt) {  // f v at u points, f u at v points (4-point averages)
@@ -412,9 +480,10 @@ __global__ void __launch_bounds__(NT) k_weno_momentum(Dims d, Phys ph, Cols c, S
   // w on face k
   float adv = 0.f;
   if (k >= 1 && k < nz) {
-    const float cw = -((xw[tz][ty][tx + 1] - xw[tz][ty][tx]) * ph.rdx + (yw[tz][ty + 1][tx] - yw[tz][ty][tx]) * ph.rdy +
-                       (zw[tz + 1][ty][tx] - zw[tz][ty][tx]) * ph.rdz);
-    adv = (cw + bw[lz][ly][lx] * (0.5f * (dzm + dc))) / (0.5f * (c.rho[k - 1] + c.rho[k]));
+    const float cw = -((S.xw[tz][ty][tx + 1] - S.xw[tz][ty][tx]) * ph.rdx +
+                       (S.yw[tz][ty + 1][tx] - S.yw[tz][ty][tx]) * ph.rdy +
+                       (S.zw[tz + 1][ty][tx] - S.zw[tz][ty][tx]) * ph.rdz);
+    adv = (cw + bw[lz][ly][lx] * (0.5f * (dzm + dc))) / (0.5f * (Lown.rm + Lown.r));
   }
   if (a.wmode == 1) {
     a.Rw[id] = adv;
