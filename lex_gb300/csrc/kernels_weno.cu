@@ -216,12 +216,108 @@ struct ScalarArgs {
   float dts;
 };
 
+// theta and qv share every mass flux, so they are staged interleaved as (theta, qv) pairs and
+// each face's two reconstructions run together on the packed FP32x2 pipe.
+typedef float2 Box2[BZ3][BY3][BX3];
+
+__device__ __forceinline__ float2 vflux6x2(float m, float2 sm3, float2 sm2, float2 sm1, float2 s0, float2 sp1,
+                                           float2 sp2, int H, int n, float2 eps) {
+  if (H <= 0 || H >= n) return f2(0.f);
+  const bool up = m >= 0.f;
+  float2 r;
+  if (H >= 3 && H <= n - 3) {
+    r = weno5x2(sel2(up, sm3, sp2), sel2(up, sm2, sp1), sel2(up, sm1, s0), sel2(up, s0, sm1), sel2(up, sp1, sm2), eps);
+  } else if (up) {
+    if (H == 1)
+      r = mul2(f2(0.5f), add2(sm1, s0));
+    else if (H == 2 || H == n - 1)
+      r = weno3x2(sm2, sm1, s0, eps);
+    else  // H == n-2
+      r = weno5x2(sm3, sm2, sm1, s0, sp1, eps);
+  } else {
+    if (H == n - 1)
+      r = mul2(f2(0.5f), add2(s0, sm1));
+    else if (H == 1 || H == n - 2)
+      r = weno3x2(sp1, s0, sm1, eps);
+    else  // H == 2
+      r = weno5x2(sp2, sp1, s0, sm1, sm2, eps);
+  }
+  return mul2(f2(m), r);
+}
+
+__device__ __forceinline__ float2 wx2(const Box2& b, int lx, int ly, int lz, float m, float2 eps) {
+  return weno_flux_x2(m, b[lz][ly][lx - 3], b[lz][ly][lx - 2], b[lz][ly][lx - 1], b[lz][ly][lx], b[lz][ly][lx + 1],
+                      b[lz][ly][lx + 2], eps);
+}
+__device__ __forceinline__ float2 wy2(const Box2& b, int lx, int ly, int lz, float m, float2 eps) {
+  return weno_flux_x2(m, b[lz][ly - 3][lx], b[lz][ly - 2][lx], b[lz][ly - 1][lx], b[lz][ly][lx], b[lz][ly + 1][lx],
+                      b[lz][ly + 2][lx], eps);
+}
+__device__ __forceinline__ float2 wz2(const Box2& b, int lx, int ly, int lz, float m, int H, int n, float2 eps) {
+  return vflux6x2(m, b[lz - 3][ly][lx], b[lz - 2][ly][lx], b[lz - 1][ly][lx], b[lz][ly][lx], b[lz + 1][ly][lx],
+                  b[lz + 2][ly][lx], H, n, eps);
+}
+
+// (theta, qv) staging: all loads in flight before the shared stores
+__device__ __forceinline__ void stage_pair(Box2& b, const float* T, const float* q, const Idx& ix, int tid,
+                                           bool vec4) {
+  if (vec4) {
+    float4 vt[IT4], vq[IT4];
+#pragma unroll
+    for (int r = 0; r < IT4; ++r) {
+      const int t = tid + r * NT;
+      if (t < NQ4) {
+        const int row = t / (BX3 / 4), c4 = t - row * (BX3 / 4);
+        const int lz = row / BY3, ly = row - lz * BY3;
+        const int g = ix.zc[lz] + ix.y[ly] + ix.x[4 * c4];
+        vt[r] = __ldg(reinterpret_cast<const float4*>(T + g));
+        vq[r] = __ldg(reinterpret_cast<const float4*>(q + g));
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < IT4; ++r) {
+      const int t = tid + r * NT;
+      if (t < NQ4) {
+        const int row = t / (BX3 / 4), c4 = t - row * (BX3 / 4);
+        const int lz = row / BY3, ly = row - lz * BY3;
+        float4* dst = reinterpret_cast<float4*>(&b[lz][ly][4 * c4]);
+        dst[0] = make_float4(vt[r].x, vq[r].x, vt[r].y, vq[r].y);
+        dst[1] = make_float4(vt[r].z, vq[r].z, vt[r].w, vq[r].w);
+      }
+    }
+  } else {
+    const int lane = tid & 31, warp = tid >> 5;
+    const int xa = ix.x[lane];
+    const bool tail = lane < BX3 - 32;
+    const int xb = tail ? ix.x[32 + lane] : 0;
+    float2 va[RPW], vb[RPW];
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+      const int row = warp + r * NWARP;
+      if (row < ROWS) {
+        const int lz = row / BY3, ly = row - lz * BY3;
+        const int base = ix.zc[lz] + ix.y[ly];
+        va[r] = make_float2(LD(T, base + xa), LD(q, base + xa));
+        vb[r] = tail ? make_float2(LD(T, base + xb), LD(q, base + xb)) : f2(0.f);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+      const int row = warp + r * NWARP;
+      if (row < ROWS) {
+        const int lz = row / BY3, ly = row - lz * BY3;
+        b[lz][ly][lane] = va[r];
+        if (tail) b[lz][ly][32 + lane] = vb[r];
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(NT) k_weno_scalars(Dims d, Phys ph, Cols c, State s, ScalarArgs a) {
-  __shared__ __align__(16) Box bT;
-  __shared__ __align__(16) Box bQ;
-  __shared__ FluxX xT, xQ;
-  __shared__ FluxY yT, yQ;
-  __shared__ FluxZ zT, zQ;
+  __shared__ __align__(16) Box2 bTQ;
+  __shared__ float2 xF[TZ][TY][TX + 1];
+  __shared__ float2 yF[TZ][TY + 1][TX];
+  __shared__ float2 zF[TZ + 1][TY][TX];
   __shared__ Idx ix;
   const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
   const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
@@ -230,12 +326,7 @@ __global__ void __launch_bounds__(NT) k_weno_scalars(Dims d, Phys ph, Cols c, St
   build_idx(ix, tid, i0, j0, k0, d);
   __syncthreads();
   // ---- every global load of the block
-  {
-    Box* const boxes[2] = {&bT, &bQ};
-    const float* const src[2] = {s.T, s.q};
-    const int* const zb[2] = {ix.zc, ix.zc};
-    stage<2>(boxes, src, zb, ix, tid, (nx & 3) == 0);
-  }
+  stage_pair(bTQ, s.T, s.q, ix, tid, (nx & 3) == 0);
   const int lx = tx + HX, ly = ty + HALO, lz = tz + HALO;
   const int k = k0 + tz;
   const bool inlev = k < nz;
@@ -273,34 +364,27 @@ __global__ void __launch_bounds__(NT) k_weno_scalars(Dims d, Phys ph, Cols c, St
   }
   __syncthreads();
   // ---- face fluxes
-  const float eT = kWepsTheta, eQ = kWepsQv;
+  const float2 eps = make_float2(kWepsTheta, kWepsQv);
   if (inlev) {
-    xT[tz][ty][tx] = wx(bT, lx, ly, lz, mx, eT);
-    xQ[tz][ty][tx] = wx(bQ, lx, ly, lz, mx, eQ);
-    yT[tz][ty][tx] = wy(bT, lx, ly, lz, my, eT);
-    yQ[tz][ty][tx] = wy(bQ, lx, ly, lz, my, eQ);
+    xF[tz][ty][tx] = wx2(bTQ, lx, ly, lz, mx, eps);
+    yF[tz][ty][tx] = wy2(bTQ, lx, ly, lz, my, eps);
   }
-  zT[tz][ty][tx] = wz(bT, lx, ly, lz, mz, k, nz, eT);  // zero outside 1..nz-1 (surface flux 0, lid)
-  zQ[tz][ty][tx] = wz(bQ, lx, ly, lz, mz, k, nz, eQ);
-  if (e.which == 0) {
-    xT[e.fk][e.fj][e.fi] = wx(bT, e.lx, e.ly, e.lz, me, eT);
-    xQ[e.fk][e.fj][e.fi] = wx(bQ, e.lx, e.ly, e.lz, me, eQ);
-  } else if (e.which == 1) {
-    yT[e.fk][e.fj][e.fi] = wy(bT, e.lx, e.ly, e.lz, me, eT);
-    yQ[e.fk][e.fj][e.fi] = wy(bQ, e.lx, e.ly, e.lz, me, eQ);
-  } else if (e.which == 2) {
-    zT[e.fk][e.fj][e.fi] = wz(bT, e.lx, e.ly, e.lz, me, He, nz, eT);
-    zQ[e.fk][e.fj][e.fi] = wz(bQ, e.lx, e.ly, e.lz, me, He, nz, eQ);
-  }
+  zF[tz][ty][tx] = wz2(bTQ, lx, ly, lz, mz, k, nz, eps);  // zero outside 1..nz-1 (surface flux 0, lid)
+  if (e.which == 0)
+    xF[e.fk][e.fj][e.fi] = wx2(bTQ, e.lx, e.ly, e.lz, me, eps);
+  else if (e.which == 1)
+    yF[e.fk][e.fj][e.fi] = wy2(bTQ, e.lx, e.ly, e.lz, me, eps);
+  else if (e.which == 2)
+    zF[e.fk][e.fj][e.fi] = wz2(bTQ, e.lx, e.ly, e.lz, me, He, nz, eps);
   __syncthreads();
   if (!own) return;
   const float r = c.rho[k];
-  const float cT = -((xT[tz][ty][tx + 1] - xT[tz][ty][tx]) * ph.rdx + (yT[tz][ty + 1][tx] - yT[tz][ty][tx]) * ph.rdy +
-                     (zT[tz + 1][ty][tx] - zT[tz][ty][tx]) * ph.rdz);
-  const float cQ = -((xQ[tz][ty][tx + 1] - xQ[tz][ty][tx]) * ph.rdx + (yQ[tz][ty + 1][tx] - yQ[tz][ty][tx]) * ph.rdy +
-                     (zQ[tz + 1][ty][tx] - zQ[tz][ty][tx]) * ph.rdz);
-  const float aT = (cT + bT[lz][ly][lx] * dv) / r;
-  const float aQ = (cQ + bQ[lz][ly][lx] * dv) / r;
+  const float2 cv = fma2(sub2(zF[tz + 1][ty][tx], zF[tz][ty][tx]), f2(-ph.rdz),
+                         fma2(sub2(yF[tz][ty + 1][tx], yF[tz][ty][tx]), f2(-ph.rdy),
+                              mul2(sub2(xF[tz][ty][tx + 1], xF[tz][ty][tx]), f2(-ph.rdx))));
+  const float2 own2 = bTQ[lz][ly][lx];
+  const float aT = (cv.x + own2.x * dv) / r;
+  const float aQ = (cv.y + own2.y * dv) / r;
   float Tn = T0 + aT * a.dts, Qn = Q0 + aQ * a.dts, rT = aT, rQ = aQ;
   if (a.sgsT) {
     Tn = Tn + sT * a.dts;

@@ -145,6 +145,71 @@ __device__ __forceinline__ float weno_flux(float m, float sm3, float sm2, float 
   return m * weno5(p ? sm3 : sp2, p ? sm2 : sp1, p ? sm1 : s0, p ? s0 : sm1, p ? sp1 : sm2, eps);
 }
 
+// ---------------------------------------------------------------------------------------------
+// two independent reconstructions at once on the packed FP32x2 pipe (sm_100+): each component
+// follows weno5 / weno3 above, with the linear weights folded into the candidate polynomials
+// (w_k q_k / sum w_k with w_k = d_k (1 + r_k^2)).  Component-wise IEEE round-to-nearest.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float2 rcp2(float2 x) { return make_float2(rcp_approx(x.x), rcp_approx(x.y)); }
+__device__ __forceinline__ float2 sel2(bool p, float2 a, float2 b) { return p ? a : b; }
+
+__device__ __forceinline__ float2 weno5x2(float2 a, float2 b, float2 c, float2 d, float2 e, float2 eps) {
+  const float2 t1 = add2(fma2(b, f2(-2.f), a), c), t2 = fma2(c, f2(3.f), fma2(b, f2(-4.f), a));
+  const float2 t3 = add2(fma2(c, f2(-2.f), b), d), t4 = sub2(b, d);
+  const float2 t5 = add2(fma2(d, f2(-2.f), c), e), t6 = fma2(d, f2(-4.f), fma2(c, f2(3.f), e));
+  const float2 b1 = fma2(mul2(t1, f2(13.f / 12.f)), t1, mul2(mul2(t2, f2(0.25f)), t2));
+  const float2 b2 = fma2(mul2(t3, f2(13.f / 12.f)), t3, mul2(mul2(t4, f2(0.25f)), t4));
+  const float2 b3 = fma2(mul2(t5, f2(13.f / 12.f)), t5, mul2(mul2(t6, f2(0.25f)), t6));
+  const float2 d13 = sub2(b1, b3);
+  const float2 tau = make_float2(fabsf(d13.x), fabsf(d13.y));
+  float2 r1 = mul2(tau, rcp2(add2(b1, eps))), r2 = mul2(tau, rcp2(add2(b2, eps))), r3 = mul2(tau, rcp2(add2(b3, eps)));
+  r1 = make_float2(fminf(kRatioCap, r1.x), fminf(kRatioCap, r1.y));
+  r2 = make_float2(fminf(kRatioCap, r2.x), fminf(kRatioCap, r2.y));
+  r3 = make_float2(fminf(kRatioCap, r3.x), fminf(kRatioCap, r3.y));
+  const float2 s1 = fma2(r1, r1, f2(1.f)), s2 = fma2(r2, r2, f2(1.f)), s3 = fma2(r3, r3, f2(1.f));
+  // d_k q_k with d = (0.1, 0.6, 0.3)
+  const float2 q1 = fma2(a, f2(0.1f * 2.f / 6.f), fma2(b, f2(0.1f * -7.f / 6.f), mul2(c, f2(0.1f * 11.f / 6.f))));
+  const float2 q2 = fma2(b, f2(0.6f * -1.f / 6.f), fma2(c, f2(0.6f * 5.f / 6.f), mul2(d, f2(0.6f * 2.f / 6.f))));
+  const float2 q3 = fma2(c, f2(0.3f * 2.f / 6.f), fma2(d, f2(0.3f * 5.f / 6.f), mul2(e, f2(0.3f * -1.f / 6.f))));
+  const float2 num = fma2(s1, q1, fma2(s2, q2, mul2(s3, q3)));
+  const float2 den = fma2(s1, f2(0.1f), fma2(s2, f2(0.6f), mul2(s3, f2(0.3f))));
+  return mul2(num, rcp2(den));
+}
+
+__device__ __forceinline__ float2 weno3x2(float2 a, float2 b, float2 c, float2 eps) {
+  const float2 dab = sub2(a, b), dbc = sub2(b, c);
+  const float2 b1 = mul2(dab, dab), b2 = mul2(dbc, dbc);
+  const float2 d12 = sub2(b1, b2);
+  const float2 tau = make_float2(fabsf(d12.x), fabsf(d12.y));
+  float2 r1 = mul2(tau, rcp2(add2(b1, eps))), r2 = mul2(tau, rcp2(add2(b2, eps)));
+  r1 = make_float2(fminf(kRatioCap, r1.x), fminf(kRatioCap, r1.y));
+  r2 = make_float2(fminf(kRatioCap, r2.x), fminf(kRatioCap, r2.y));
+  const float2 s1 = fma2(r1, r1, f2(1.f)), s2 = fma2(r2, r2, f2(1.f));
+  const float2 q1 = fma2(a, f2(-0.5f / 3.f), mul2(b, f2(1.5f / 3.f)));        // (1/3)(-a/2 + 3b/2)
+  const float2 q2 = fma2(b, f2(0.5f * 2.f / 3.f), mul2(c, f2(0.5f * 2.f / 3.f)));  // (2/3)(b/2 + c/2)
+  const float2 num = fma2(s1, q1, mul2(s2, q2));
+  const float2 den = fma2(s1, f2(1.f / 3.f), mul2(s2, f2(2.f / 3.f)));
+  return mul2(num, rcp2(den));
+}
+
+// m * upwind WENO5 value for two fields sharing the mass flux m (see weno_flux)
+__device__ __forceinline__ float2 weno_flux_x2(float m, float2 sm3, float2 sm2, float2 sm1, float2 s0, float2 sp1,
+                                               float2 sp2, float2 eps) {
+  const bool p = m >= 0.f;
+  return mul2(f2(m), weno5x2(sel2(p, sm3, sp2), sel2(p, sm2, sp1), sel2(p, sm1, s0), sel2(p, s0, sm1),
+                             sel2(p, sp1, sm2), eps));
+}
+
 // m * (upwind vertical face value) at face f of an n-entry column (see vrecon); zero at the ends.
 template <class F>
 __device__ __forceinline__ float vflux(float m, const F& s, int f, int n, float eps) {

@@ -98,6 +98,26 @@ def pad_v(a):
     return np.concatenate((a[:, :, :1], a, a[:, :, -1:]), axis=2)
 
 
+def random_state(phys, nx, ny, nz, seed):
+    """A random padded state around a warm-bubble state ``phys``: theta + N(0, 0.5 K), u and v
+    N(0, 2 m/s), w N(0, 1 m/s) with zero end faces, pi' N(0, 1e-4), qv (1 + N(0, 0.05)).
+    Halos filled as the reference's padding functions do."""
+    rng = np.random.default_rng(seed)
+    rnd = lambda shape, s: rng.standard_normal(shape) * s
+    th = pad_scalar(phys[0][3:-3, 3:-3, 1:-1] + rnd((nx, ny, nz), 0.5))
+    ui = rnd((nx, ny, nz), 2.0)
+    u = pad_u(np.concatenate([ui, ui[:1]], 0))
+    vi = rnd((nx, ny, nz), 2.0)
+    v = pad_v(np.concatenate([vi, vi[:, :1]], 1))
+    wi = rnd((nx, ny, nz + 1), 1.0)
+    wi[:, :, 0] = 0.0
+    wi[:, :, -1] = 0.0
+    w = pad_scalar(wi)
+    pip = pad_scalar(rnd((nx, ny, nz), 1e-4))
+    qv = pad_scalar(phys[5][3:-3, 3:-3, 1:-1] * (1.0 + rnd((nx, ny, nz), 0.05)))
+    return (th, u, v, w, pip, qv)
+
+
 def hydrostatic_columns(theta0_col, qv0_col, dz):
     """FP64 hydrostatic base state on the padded column (setup_lex.py:123-132).
 

@@ -30,7 +30,7 @@ sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 import jax_standin as js  # noqa: E402
-from oracle.ic import WarmBubble, pad_scalar, pad_u, pad_v  # noqa: E402
+from oracle.ic import WarmBubble, random_state  # noqa: E402
 
 MODEL_OPT = (2, False, False, 0, False, False, 1)   # solver 2, Smagorinsky on, all else off
 FIELDS = ("theta", "u", "v", "w", "pip", "qv")
@@ -40,23 +40,6 @@ def set_namelist(nl, nx, ny, nz, dx, dy, dz, dt, n_sound=32):
     nl.nx, nl.ny, nl.nz, nl.dx, nl.dy, nl.dz, nl.dt = nx, ny, nz, dx, dy, dz, dt
     nl.n_sound = n_sound
     nl.solver_opt, nl.turb_opt = 2, 1
-
-
-def random_state(phys, nx, ny, nz, seed):
-    rng = np.random.default_rng(seed)
-    rnd = lambda shape, s: rng.standard_normal(shape) * s
-    th = pad_scalar(phys[0][3:-3, 3:-3, 1:-1] + rnd((nx, ny, nz), 0.5))
-    ui = rnd((nx, ny, nz), 2.0)
-    u = pad_u(np.concatenate([ui, ui[:1]], 0))
-    vi = rnd((nx, ny, nz), 2.0)
-    v = pad_v(np.concatenate([vi, vi[:, :1]], 1))
-    wi = rnd((nx, ny, nz + 1), 1.0)
-    wi[:, :, 0] = 0.0
-    wi[:, :, -1] = 0.0
-    w = pad_scalar(wi)
-    pip = pad_scalar(rnd((nx, ny, nz), 1e-4))
-    qv = pad_scalar(phys[5][3:-3, 3:-3, 1:-1] * (1.0 + rnd((nx, ny, nz), 0.05)))
-    return (th, u, v, w, pip, qv)
 
 
 def columns(base):
