@@ -165,7 +165,7 @@ int run_stage(lexgb_ctx* c, int s, const State& xi0, const State& xis, const Sta
   AcousticIn in{xi0.u, xi0.v, xi0.w, xi0.p, c->Ru, c->Rv, c->Rw, c->trho, xis.p};
   const AcousticOut X{c->Xu, c->Xv, c->Xw, c->Xp}, Y{c->Yu, c->Yv, c->Yw, c->Yp};
   const AcousticOut O{out.u, out.v, out.w, out.p};
-  const bool pairs = c->cfg.acoustic_pairs != 0;
+  const bool pairs = c->cfg.acoustic_pairs != 0 && c->d.nx % 4 == 0;  // the pair kernel needs nx % 4 == 0
   const int nsingle = pairs ? (n & 1) : n;
   const int launches = nsingle + (pairs ? n / 2 : 0);
   const bool alias = (out.u == xi0.u);

@@ -29,10 +29,10 @@ def _case(nx, ny, nz, seed=5):
     return (dx, dy, dz, dt), cols, state, D
 
 
-def _solver(nx, ny, nz, geom, cols):
+def _solver(nx, ny, nz, geom, cols, pairs=False):
     from lex_gb300.solver import Solver
     dx, dy, dz, dt = geom
-    S = Solver(nx, ny, nz, dx, dy, dz, dt, 32, turb_opt=1)
+    S = Solver(nx, ny, nz, dx, dy, dz, dt, 32, turb_opt=1, acoustic_pairs=pairs)
     S.set_base_columns(cols["theta0"], cols["qv0"], cols["pi0"], cols["rho0"])
     return S
 
@@ -75,11 +75,12 @@ def test_operators_on_ragged_grid(built_lib, nx, ny, nz):
     assert not bad, bad
 
 
+@pytest.mark.parametrize("pairs", [False, True], ids=["one_substep_per_launch", "two_substeps_per_launch"])
 @pytest.mark.parametrize("nx,ny,nz", GRIDS, ids=["%dx%dx%d" % g for g in GRIDS])
-def test_step_on_ragged_grid(built_lib, nx, ny, nz):
+def test_step_on_ragged_grid(built_lib, nx, ny, nz, pairs):
     geom, cols, state, D = _case(nx, ny, nz)
     nxt, _ = D.step(state)
-    with _solver(nx, ny, nz, geom, cols) as S:
+    with _solver(nx, ny, nz, geom, cols, pairs) as S:
         S.upload(state)
         S.step(1)
         out = S.download()
