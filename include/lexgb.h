@@ -178,6 +178,20 @@ int lexgb_budget_noalloc(int nx, int ny, int nz, double dx, double dy, double dz
                          double *out, void *stream);
 
 /* Message of the last failure on this thread; returns the untruncated length. */
+/* Reverse mode (vector-Jacobian product) of the first `nstages` (1..3) WS-RK3 stages of one big
+ * step taken from the resident state: given ybar, the adjoint of the state after those stages,
+ * writes xbar, the adjoint of the resident state.  The resident state is not modified.  The
+ * forward stages are recomputed internally and every intermediate the reverse pass needs (stage
+ * states, divergence, theta_rho, slow tendencies and all acoustic sub-step states) is kept in a
+ * workspace allocated on first use (about 110 + 4 * (acoustic sub-steps per step) fields).
+ * Arrays are interior-only in the device layout, x fastest: theta, u, v, pi', qv [nz][ny][nx],
+ * w [nz+1][ny][nx] (u on west faces, v on south faces, w on faces 0..nz), FP32, host pointers
+ * (on_device = 0) or device pointers (on_device = 1).
+ * Replaces jax.vjp of ws_rk3_big_step (one_sprint_functions.py:10-30) as used by the training
+ * loop (lex_dl_train.py:114).  Requires turb_opt = 0 (the Smagorinsky terms have no reverse mode
+ * yet: LEXGB_ERR_ARG). */
+int lexgb_step_vjp(lexgb_ctx *ctx, int nstages, const float *const ybar[6], float *xbar[6], int on_device);
+
 int lexgb_last_error(char *buf, size_t len);
 
 #ifdef __cplusplus

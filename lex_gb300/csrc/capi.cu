@@ -7,10 +7,11 @@
 #include <string.h>
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/lexgb.h"
-#include "lexgb_internal.cuh"
+#include "lexgb_adjoint.cuh"
 
 using namespace lexgb;
 
@@ -80,6 +81,8 @@ struct lexgb_ctx {
   double* partial = nullptr;
   double* budget = nullptr;
   unsigned long long* count = nullptr;
+  // reverse mode: workspace of the recomputed step and the adjoint fields (allocated on first use)
+  float* adj_arena = nullptr;
   // graph of one big step
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -371,6 +374,7 @@ int lexgb_destroy(lexgb_ctx* c) {
   drop_graph(c);
   cudaFree(c->arena);
   cudaFree(c->rec_arena);
+  cudaFree(c->adj_arena);
   cudaFree(c->base64);
   cudaFree(c->tab);
   cudaFree(c->stage);
@@ -723,6 +727,167 @@ int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   *ms_per_launch = ms / reps;
+  return LEXGB_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// reverse mode
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+struct AdjWork {
+  State S[4];            // stage outputs S[1..3] (u, v, w, p alias the last acoustic state of the stage)
+  float *div[3], *trho[3], *Ru[3], *Rv[3], *Rw[3];
+  float* ac[3][64][4];   // acoustic states 1..n of each stage: u, v, w, p
+  State Xb0, Cur, Xs;    // adjoints: step input, current stage output, current stage input
+  float* pp[2][4];       // acoustic adjoint ping-pong
+  float *Rub, *Rvb, *Rwb, *trhob, *psb;
+  float* cb[5];
+  float* divb;
+  float* P[5][6];
+  float* mb[4];
+  float* sgsb[5];
+};
+
+int adj_fields(const StagePlan& p) { return 6 + 15 + 4 * (p.n[0] + p.n[1] + p.n[2]) + 18 + 8 + 5 + 6 + 34 + 5; }
+
+int ensure_adjoint(lexgb_ctx* c, AdjWork& w) {
+  const StagePlan p = plan_of(c->cfg);
+  if (p.n[0] > 64 || p.n[1] > 64 || p.n[2] > 64) return fail(LEXGB_ERR_ARG, "adjoint supports up to 64 acoustic sub-steps per stage");
+  const size_t nf = adj_fields(p);
+  if (!c->adj_arena) {
+    cudaError_t e = cudaMalloc(&c->adj_arena, nf * c->fstride * sizeof(float));
+    if (e != cudaSuccess) return fail(LEXGB_ERR_ALLOC, std::string("adjoint workspace: ") + cudaGetErrorString(e));
+  }
+  float* q = c->adj_arena;
+  auto take = [&]() {
+    float* r = q;
+    q += c->fstride;
+    return r;
+  };
+  for (int s = 0; s < 3; ++s) {
+    w.div[s] = take(); w.trho[s] = take(); w.Ru[s] = take(); w.Rv[s] = take(); w.Rw[s] = take();
+    for (int m = 1; m <= p.n[s]; ++m)
+      for (int f = 0; f < 4; ++f) w.ac[s][m][f] = take();
+    State& o = w.S[s + 1];
+    o.T = take();
+    o.q = take();
+    o.u = w.ac[s][p.n[s]][0]; o.v = w.ac[s][p.n[s]][1]; o.w = w.ac[s][p.n[s]][2]; o.p = w.ac[s][p.n[s]][3];
+  }
+  w.Xb0 = fields_at(take(), c->fstride); for (int i = 1; i < NFIELD; ++i) take();
+  w.Cur = fields_at(take(), c->fstride); for (int i = 1; i < NFIELD; ++i) take();
+  w.Xs = fields_at(take(), c->fstride); for (int i = 1; i < NFIELD; ++i) take();
+  for (int a = 0; a < 2; ++a) for (int f = 0; f < 4; ++f) w.pp[a][f] = take();
+  w.Rub = take(); w.Rvb = take(); w.Rwb = take(); w.trhob = take(); w.psb = take();
+  for (int f = 0; f < 5; ++f) w.cb[f] = take();
+  w.divb = take();
+  for (int f = 0; f < 5; ++f) for (int s = 0; s < 6; ++s) w.P[f][s] = take();
+  for (int f = 0; f < 4; ++f) w.mb[f] = take();
+  for (int f = 0; f < 5; ++f) w.sgsb[f] = take();
+  if ((size_t)(q - c->adj_arena) > nf * c->fstride) return fail(LEXGB_ERR_STATE, "adjoint workspace layout");
+  return LEXGB_OK;
+}
+
+int zero_state(lexgb_ctx* c, const State& s) {
+  for (int f = 0; f < NFIELD; ++f) CK(cudaMemsetAsync(field_of(s, f), 0, c->fstride * sizeof(float), c->stream));
+  return LEXGB_OK;
+}
+
+}  // namespace
+
+int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float* xbar[6], int on_device) {
+  CKS(check_ready(c));
+  if (nstages < 1 || nstages > 3 || !ybar || !xbar) return fail(LEXGB_ERR_ARG, "need 1..3 stages, ybar and xbar");
+  for (int f = 0; f < 6; ++f)
+    if (!ybar[f] || !xbar[f]) return fail(LEXGB_ERR_ARG, "null field pointer");
+  if (c->cfg.turb_opt != 0) return fail(LEXGB_ERR_ARG, "reverse mode of the Smagorinsky terms is not built: use turb_opt 0");
+  AdjWork w;
+  CKS(ensure_adjoint(c, w));
+  const Dims& d = c->d;
+  const StagePlan p = plan_of(c->cfg);
+  const State& A = c->A;
+  const Sgs none{nullptr, nullptr, nullptr, nullptr, nullptr};
+  // ---- forward, keeping every intermediate the reverse pass reads
+  for (int s = 0; s < nstages; ++s) {
+    const State xs = s == 0 ? A : w.S[s];
+    const State& out = w.S[s + 1];
+    CK(launch_div_trho(d, c->ph, c->cols, xs, w.div[s], w.trho[s], c->stream));
+    SlowOut so{nullptr, nullptr, nullptr, out.T, out.q, nullptr, nullptr};
+    CK(launch_adv_scalars(d, c->ph, c->cols, xs, w.div[s], A.T, A.q, none, (float)p.dts[s], so, c->stream));
+    CK(launch_adv_momentum(d, c->ph, c->cols, xs, w.div[s], none, w.Ru[s], w.Rv[s], w.Rw[s], 0, c->stream));
+    AcousticIn in{A.u, A.v, A.w, A.p, w.Ru[s], w.Rv[s], w.Rw[s], w.trho[s], xs.p};
+    for (int m = 1; m <= p.n[s]; ++m) {
+      const AcousticOut o{w.ac[s][m][0], w.ac[s][m][1], w.ac[s][m][2], w.ac[s][m][3]};
+      CK(launch_acoustic(d, c->ph, c->cols, in, o, (float)p.dtau[s], c->stream));
+      in.u = o.u; in.v = o.v; in.w = o.w; in.p = o.p;
+    }
+  }
+  // ---- seed
+  const size_t cells = (size_t)d.cells(), faces = (size_t)d.faces();
+  for (int f = 0; f < 6; ++f) {
+    const size_t n = (f == 3 ? faces : cells) * sizeof(float);
+    CK(cudaMemsetAsync(field_of(w.Cur, f), 0, c->fstride * sizeof(float), c->stream));
+    CK(cudaMemcpyAsync(field_of(w.Cur, f), ybar[f], n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                       c->stream));
+  }
+  CKS(zero_state(c, w.Xb0));
+  // ---- reverse
+  for (int s = nstages - 1; s >= 0; --s) {
+    const State xs = s == 0 ? A : w.S[s];
+    CKS(zero_state(c, w.Xs));
+    for (float* z : {w.Rub, w.Rvb, w.Rwb, w.trhob, w.psb})
+      CK(cudaMemsetAsync(z, 0, c->fstride * sizeof(float), c->stream));
+    // acoustic loop backwards
+    const float* adj[4] = {w.Cur.u, w.Cur.v, w.Cur.w, w.Cur.p};
+    for (int m = p.n[s], k = 0; m >= 1; --m, ++k) {
+      float* const* o = w.pp[k & 1];
+      const float* oldp = m == 1 ? A.p : w.ac[s][m - 1][3];
+      AcousticVjpArgs a{oldp, w.trho[s], xs.p, w.ac[s][m][0], w.ac[s][m][1], w.ac[s][m][2],
+                        adj[0], adj[1], adj[2], adj[3], o[0], o[1], o[2], o[3],
+                        w.Rub, w.Rvb, w.Rwb, w.trhob, w.psb};
+      CK(launch_acoustic_vjp(d, c->ph, c->cols, a, (float)p.dtau[s], c->stream));
+      for (int f = 0; f < 4; ++f) adj[f] = o[f];
+    }
+    CK(launch_axpy(w.Xb0.u, adj[0], faces, c->stream));
+    CK(launch_axpy(w.Xb0.v, adj[1], faces, c->stream));
+    CK(launch_axpy(w.Xb0.w, adj[2], faces, c->stream));
+    CK(launch_axpy(w.Xb0.p, adj[3], faces, c->stream));
+    // slow tendencies, theta/qv update, theta_rho, pi'_s
+    StageVjpArgs sa{};
+    sa.xs = xs;
+    sa.div = w.div[s];
+    sa.Tnb = w.Cur.T;
+    sa.qnb = w.Cur.q;
+    sa.Rub = w.Rub; sa.Rvb = w.Rvb; sa.Rwb = w.Rwb; sa.trhob = w.trhob; sa.psb = w.psb;
+    sa.dts = (float)p.dts[s];
+    sa.xsb = w.Xs;
+    sa.x0b = w.Xb0;
+    for (int f = 0; f < 5; ++f) sa.cb[f] = w.cb[f];
+    sa.divb = w.divb;
+    CK(launch_stage_pointwise_vjp(d, c->ph, c->cols, sa, c->stream));
+    AdvVjpArgs aa{};
+    aa.xs = xs;
+    aa.phi[0] = xs.u; aa.phi[1] = xs.v; aa.phi[2] = xs.w; aa.phi[3] = xs.T; aa.phi[4] = xs.q;
+    for (int f = 0; f < 5; ++f) {
+      aa.cb[f] = w.cb[f];
+      for (int q = 0; q < 6; ++q) aa.P[f][q] = w.P[f][q];
+    }
+    for (int f = 0; f < 4; ++f) aa.mb[f] = w.mb[f];
+    aa.xsb = w.Xs;
+    CK(launch_adv_vjp(d, c->ph, c->cols, aa, c->stream));
+    CK(launch_massdiv_vjp(d, c->ph, c->cols, w.divb, w.Xs, c->stream));
+    if (s == 0) {
+      for (int f = 0; f < NFIELD; ++f) CK(launch_axpy(field_of(w.Xb0, f), field_of(w.Xs, f), faces, c->stream));
+    } else {
+      std::swap(w.Cur, w.Xs);
+    }
+  }
+  for (int f = 0; f < 6; ++f) {
+    const size_t n = (f == 3 ? faces : cells) * sizeof(float);
+    CK(cudaMemcpyAsync(xbar[f], field_of(w.Xb0, f), n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                       c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
   return LEXGB_OK;
 }
 

@@ -1,0 +1,527 @@
+// kernels_adjoint.cu - vector-Jacobian products (reverse mode) of the big-step operators.
+//
+// Every kernel is a gather: a thread owns one output adjoint value and sums the contributions
+// of the forward outputs that depend on it, so there are no atomics and the results do not
+// depend on scheduling.  The forward operators and their reference counterparts:
+//
+//   acoustic sub-step        one_step_integration.py:519-556 (k_acoustic_vec)
+//   WENO flux divergence     advection.py:9-149, fluxes :305-1281 (k_weno_scalars/momentum)
+//   mass divergence          advection.py:200-226 (k_div_trho)
+//   theta_rho, buoyancy      one_step_integration.py:269, pressure_equations.py:162-172
+//   Coriolis                 pressure_gradient_coriolis.py:80-113
+//
+// WENO adjoint: for each direction a face kernel evaluates, for every flux of the five advected
+// fields (theta, qv, u, v, w), the flux adjoint Fbar = (cbar(right) - cbar(left)) / dx, the
+// reconstruction W and its derivatives with respect to its stencil, and stores
+// Fbar * m * dW/ds as six slots (the cells p-3 .. p+2 of the flux between p-1 and p) plus the
+// mass-flux adjoint Fbar * W.  A gather kernel then adds, for every point, the six slots that
+// name it and the mass-flux adjoints of the fluxes whose mass flux it enters.
+#include "lexgb_adjoint.cuh"
+
+namespace lexgb {
+
+namespace {
+
+constexpr int AB = 256;
+#define LD(p, idx) __ldg((p) + (idx))
+
+constexpr float kHalfCp = (float)(0.5 * kCp);
+constexpr float kRdCvA = (float)(kRd / kCv);
+
+__device__ __forceinline__ int wrapx(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// ---------------------------------------------------------------------------------------------
+// reconstruction derivatives
+// ---------------------------------------------------------------------------------------------
+// W = weno5(a..e) (same formulas as weno5 in lexgb_internal.cuh) and dW/d(a..e) into g[0..4].
+__device__ __forceinline__ float weno5_grad(float a, float b, float c, float d, float e, float eps, float* g) {
+  const float t1 = a - 2.f * b + c, t2 = a - 4.f * b + 3.f * c;
+  const float t3 = b - 2.f * c + d, t4 = b - d;
+  const float t5 = c - 2.f * d + e, t6 = 3.f * c - 4.f * d + e;
+  const float b1 = (13.f / 12.f) * t1 * t1 + 0.25f * t2 * t2;
+  const float b2 = (13.f / 12.f) * t3 * t3 + 0.25f * t4 * t4;
+  const float b3 = (13.f / 12.f) * t5 * t5 + 0.25f * t6 * t6;
+  const float dd = b1 - b3, tau = fabsf(dd), sg = dd >= 0.f ? 1.f : -1.f;
+  const float e1 = b1 + eps, e2 = b2 + eps, e3 = b3 + eps;
+  const float q1r = tau / e1, q2r = tau / e2, q3r = tau / e3;
+  const float r1 = fminf(kRatioCap, q1r), r2 = fminf(kRatioCap, q2r), r3 = fminf(kRatioCap, q3r);
+  const float w1 = 0.1f * (1.f + r1 * r1), w2 = 0.6f * (1.f + r2 * r2), w3 = 0.3f * (1.f + r3 * r3);
+  const float q1 = (2.f / 6.f) * a + (-7.f / 6.f) * b + (11.f / 6.f) * c;
+  const float q2 = (-1.f / 6.f) * b + (5.f / 6.f) * c + (2.f / 6.f) * d;
+  const float q3 = (2.f / 6.f) * c + (5.f / 6.f) * d + (-1.f / 6.f) * e;
+  const float S = w1 + w2 + w3, iS = 1.f / S;
+  const float W = (w1 * q1 + w2 * q2 + w3 * q3) * iS;
+  // reverse
+  const float qb1 = w1 * iS, qb2 = w2 * iS, qb3 = w3 * iS;
+  const float wb1 = (q1 - W) * iS, wb2 = (q2 - W) * iS, wb3 = (q3 - W) * iS;
+  const float rb1 = q1r < kRatioCap ? wb1 * 0.2f * r1 : 0.f;
+  const float rb2 = q2r < kRatioCap ? wb2 * 1.2f * r2 : 0.f;
+  const float rb3 = q3r < kRatioCap ? wb3 * 0.6f * r3 : 0.f;
+  const float taub = rb1 / e1 + rb2 / e2 + rb3 / e3;
+  const float bb1 = -rb1 * r1 / e1 + taub * sg;
+  const float bb2 = -rb2 * r2 / e2;
+  const float bb3 = -rb3 * r3 / e3 - taub * sg;
+  const float tb1 = bb1 * (13.f / 6.f) * t1, tb2 = bb1 * 0.5f * t2;
+  const float tb3 = bb2 * (13.f / 6.f) * t3, tb4 = bb2 * 0.5f * t4;
+  const float tb5 = bb3 * (13.f / 6.f) * t5, tb6 = bb3 * 0.5f * t6;
+  g[0] = tb1 + tb2 + (2.f / 6.f) * qb1;
+  g[1] = -2.f * tb1 - 4.f * tb2 + tb3 + tb4 + (-7.f / 6.f) * qb1 + (-1.f / 6.f) * qb2;
+  g[2] = tb1 + 3.f * tb2 - 2.f * tb3 + tb5 + 3.f * tb6 + (11.f / 6.f) * qb1 + (5.f / 6.f) * qb2 + (2.f / 6.f) * qb3;
+  g[3] = tb3 - tb4 - 2.f * tb5 - 4.f * tb6 + (2.f / 6.f) * qb2 + (5.f / 6.f) * qb3;
+  g[4] = tb5 + tb6 + (-1.f / 6.f) * qb3;
+  return W;
+}
+
+// W = weno3(a, b, c) and dW/d(a, b, c) into g[0..2].
+__device__ __forceinline__ float weno3_grad(float a, float b, float c, float eps, float* g) {
+  const float dab = a - b, dbc = b - c;
+  const float b1 = dab * dab, b2 = dbc * dbc;
+  const float dd = b1 - b2, tau = fabsf(dd), sg = dd >= 0.f ? 1.f : -1.f;
+  const float e1 = b1 + eps, e2 = b2 + eps;
+  const float q1r = tau / e1, q2r = tau / e2;
+  const float r1 = fminf(kRatioCap, q1r), r2 = fminf(kRatioCap, q2r);
+  const float w1 = (1.f / 3.f) * (1.f + r1 * r1), w2 = (2.f / 3.f) * (1.f + r2 * r2);
+  const float q1 = -0.5f * a + 1.5f * b, q2 = 0.5f * b + 0.5f * c;
+  const float iS = 1.f / (w1 + w2);
+  const float W = (w1 * q1 + w2 * q2) * iS;
+  const float qb1 = w1 * iS, qb2 = w2 * iS;
+  const float wb1 = (q1 - W) * iS, wb2 = (q2 - W) * iS;
+  const float rb1 = q1r < kRatioCap ? wb1 * (2.f / 3.f) * r1 : 0.f;
+  const float rb2 = q2r < kRatioCap ? wb2 * (4.f / 3.f) * r2 : 0.f;
+  const float taub = rb1 / e1 + rb2 / e2;
+  const float bb1 = -rb1 * r1 / e1 + taub * sg;
+  const float bb2 = -rb2 * r2 / e2 - taub * sg;
+  g[0] = bb1 * 2.f * dab - 0.5f * qb1;
+  g[1] = -bb1 * 2.f * dab + bb2 * 2.f * dbc + 1.5f * qb1 + 0.5f * qb2;
+  g[2] = -bb2 * 2.f * dbc + 0.5f * qb2;
+  return W;
+}
+
+// Lateral face between s[2] and s[3] of s[0..5] (cells p-3 .. p+2): W and dW/ds into g[0..5].
+__device__ __forceinline__ float lateral_grad(float m, const float* s, float eps, float* g) {
+  float h[5];
+  for (int q = 0; q < 6; ++q) g[q] = 0.f;
+  if (m >= 0.f) {
+    const float W = weno5_grad(s[0], s[1], s[2], s[3], s[4], eps, h);
+    for (int q = 0; q < 5; ++q) g[q] = h[q];
+    return W;
+  }
+  const float W = weno5_grad(s[5], s[4], s[3], s[2], s[1], eps, h);
+  for (int q = 0; q < 5; ++q) g[5 - q] = h[q];
+  return W;
+}
+
+// Vertical face H of an n-entry column (between entries H-1 and H), s[0..5] = entries H-3 .. H+2
+// (entries outside 0..n-1 are never used); rules of vflux6 in kernels_weno.cu.
+__device__ __forceinline__ float vertical_grad(float m, const float* s, int H, int n, float eps, float* g) {
+  float h[5];
+  for (int q = 0; q < 6; ++q) g[q] = 0.f;
+  if (H <= 0 || H >= n) return 0.f;
+  const bool up = m >= 0.f;
+  if (H >= 3 && H <= n - 3) return lateral_grad(m, s, eps, g);
+  if (up) {
+    if (H == 1) {
+      g[2] = 0.5f;
+      g[3] = 0.5f;
+      return 0.5f * (s[2] + s[3]);
+    }
+    if (H == 2 || H == n - 1) {
+      const float W = weno3_grad(s[1], s[2], s[3], eps, h);
+      g[1] = h[0]; g[2] = h[1]; g[3] = h[2];
+      return W;
+    }
+    const float W = weno5_grad(s[0], s[1], s[2], s[3], s[4], eps, h);  // H == n-2
+    for (int q = 0; q < 5; ++q) g[q] = h[q];
+    return W;
+  }
+  if (H == n - 1) {
+    g[3] = 0.5f;
+    g[2] = 0.5f;
+    return 0.5f * (s[3] + s[2]);
+  }
+  if (H == 1 || H == n - 2) {
+    const float W = weno3_grad(s[4], s[3], s[2], eps, h);
+    g[4] = h[0]; g[3] = h[1]; g[2] = h[2];
+    return W;
+  }
+  const float W = weno5_grad(s[5], s[4], s[3], s[2], s[1], eps, h);  // H == 2
+  for (int q = 0; q < 5; ++q) g[5 - q] = h[q];
+  return W;
+}
+
+// ---------------------------------------------------------------------------------------------
+// acoustic sub-step
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(AB) k_acoustic_vjp(Dims d, Phys ph, Cols c, AcousticVjpArgs a, float dtau) {
+  const long long t = (long long)blockIdx.x * AB + threadIdx.x;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
+  if (t >= d.cells()) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
+  const int im = wrapx(i - 1, nx), ip = wrapx(i + 1, nx), jm = wrapx(j - 1, ny), jp = wrapx(j + 1, ny);
+  const int id = (int)t, row = k * plane + j * nx;
+  const int cW = row + im, cE = row + ip, cS = k * plane + jm * nx + i, cN = k * plane + jp * nx + i;
+  const int cB = id - plane, cT = id + plane;
+  const bool hb = k > 0, ht = k + 1 < nz;
+  const float rdx = ph.rdx, rdy = ph.rdy, rdz = ph.rdz;
+  const float K = kDivDamp * dtau;
+  auto Aof = [&](int q) { return K * LD(a.pnb, q); };
+  auto divb = [&](int q, int kk, float A) { return -A * kRdCvA * (c.pi0[kk] + LD(a.ps, q)); };
+  const float A0 = Aof(id), AW = Aof(cW), AE = Aof(cE), AS = Aof(cS), AN = Aof(cN);
+  const float AB_ = hb ? Aof(cB) : 0.f, AT = ht ? Aof(cT) : 0.f;
+  const float s0 = LD(a.ps, id), sW = LD(a.ps, cW), sE = LD(a.ps, cE), sS = LD(a.ps, cS), sN = LD(a.ps, cN);
+  const float sB = hb ? LD(a.ps, cB) : 0.f, sT = ht ? LD(a.ps, cT) : 0.f;
+  const float D0 = divb(id, k, A0), DW = divb(cW, k, AW), DE = divb(cE, k, AE), DS = divb(cS, k, AS),
+              DN = divb(cN, k, AN);
+  const float DB = hb ? divb(cB, k - 1, AB_) : 0.f, DT = ht ? divb(cT, k + 1, AT) : 0.f;
+  // adjoints of the new winds on the six faces of the cell
+  const float Gw = (s0 - sW) * rdx, Ge = (sE - s0) * rdx, Gs = (s0 - sS) * rdy, Gn = (sN - s0) * rdy;
+  const float Uw = LD(a.unb, id) + (DW - D0) * rdx - 0.5f * Gw * (A0 + AW);
+  const float Ue = LD(a.unb, cE) + (D0 - DE) * rdx - 0.5f * Ge * (AE + A0);
+  const float Vs = LD(a.vnb, id) + (DS - D0) * rdy - 0.5f * Gs * (A0 + AS);
+  const float Vn = LD(a.vnb, cN) + (D0 - DN) * rdy - 0.5f * Gn * (AN + A0);
+  const float rho = c.rho[k];
+  float Wb = 0.f, Wt = 0.f;
+  if (hb) {
+    const float Z = c.dpi0dz[k] + (s0 - sB) * rdz;
+    Wb = LD(a.wnb, id) + (DB - D0) * rdz - 0.5f * Z * c.rho_face[k] * (A0 / rho + AB_ / c.rho[k - 1]);
+  }
+  if (ht) {
+    const float Z = c.dpi0dz[k + 1] + (sT - s0) * rdz;
+    Wt = LD(a.wnb, cT) + (D0 - DT) * rdz - 0.5f * Z * c.rho_face[k + 1] * (AT / c.rho[k + 1] + A0 / rho);
+  }
+  // old winds: identity; slow tendencies: dtau
+  a.ub[id] = Uw;
+  a.vb[id] = Vs;
+  a.wb[id] = Wb;
+  if (k == nz - 1) a.wb[id + plane] = 0.f;
+  a.Rub[id] += Uw * dtau;
+  a.Rvb[id] += Vs * dtau;
+  if (hb) a.Rwb[id] += Wb * dtau;
+  // pressure-gradient terms: pi' and theta_rho of the old state
+  const float p0 = LD(a.p, id), t0 = LD(a.trho, id);
+  const float c0 = -kHalfCp * dtau;
+  float pb = LD(a.pnb, id), tb = 0.f;
+  {
+    const float pw = LD(a.p, cW), tw = LD(a.trho, cW), pe = LD(a.p, cE), te = LD(a.trho, cE);
+    pb += Uw * c0 * (t0 + tw) * rdx - Ue * c0 * (te + t0) * rdx;
+    tb += Uw * c0 * (p0 - pw) * rdx + Ue * c0 * (pe - p0) * rdx;
+    const float ps_ = LD(a.p, cS), ts = LD(a.trho, cS), pn = LD(a.p, cN), tn = LD(a.trho, cN);
+    pb += Vs * c0 * (t0 + ts) * rdy - Vn * c0 * (tn + t0) * rdy;
+    tb += Vs * c0 * (p0 - ps_) * rdy + Vn * c0 * (pn - p0) * rdy;
+    if (hb) {
+      const float pbm = LD(a.p, cB), tbm = LD(a.trho, cB);
+      pb += Wb * c0 * (t0 + tbm) * rdz;
+      tb += Wb * c0 * (p0 - pbm) * rdz;
+    }
+    if (ht) {
+      const float ptp = LD(a.p, cT), ttp = LD(a.trho, cT);
+      pb -= Wt * c0 * (ttp + t0) * rdz;
+      tb += Wt * c0 * (ptp - p0) * rdz;
+    }
+  }
+  a.pb[id] = pb;
+  a.trhob[id] += tb;
+  // pi'_s: the divergence factor and advection_pi of this cell and its six neighbours
+  const float uw = LD(a.un, id), ue = LD(a.un, cE), vs = LD(a.vn, id), vn = LD(a.vn, cN);
+  const float wbn = hb ? LD(a.wn, id) : 0.f, wtn = ht ? LD(a.wn, cT) : 0.f;
+  const float div = (ue - uw) * rdx + (vn - vs) * rdy + (wtn - wbn) * rdz;
+  const float dap = -(0.5f * (-ue * rdx + uw * rdx) + 0.5f * (-vn * rdy + vs * rdy) +
+                      ((hb ? 0.5f * c.rho_face[k] * wbn * rdz : 0.f) - (ht ? 0.5f * c.rho_face[k + 1] * wtn * rdz : 0.f)) /
+                          rho);
+  float sb = A0 * (-kRdCvA * div + dap);
+  sb += AE * 0.5f * ue * rdx - AW * 0.5f * uw * rdx;
+  sb += AN * 0.5f * vn * rdy - AS * 0.5f * vs * rdy;
+  if (ht) sb += AT * 0.5f * c.rho_face[k + 1] * wtn * rdz / c.rho[k + 1];
+  if (hb) sb -= AB_ * 0.5f * c.rho_face[k] * wbn * rdz / c.rho[k - 1];
+  a.psb[id] += sb;
+}
+
+// ---------------------------------------------------------------------------------------------
+// pointwise part of a stage's reverse pass (after the acoustic loop):
+//   cbar of the five advected fields, the phi*div terms, Coriolis, buoyancy, theta_rho,
+//   pi'_s, SGS adjoints and the identity paths to xi0
+// ---------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(AB) k_stage_pointwise_vjp(Dims d, Phys ph, Cols c, StageVjpArgs a) {
+  const long long t = (long long)blockIdx.x * AB + threadIdx.x;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
+  if (t >= d.faces()) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
+  const int id = (int)t;
+  const int im = wrapx(i - 1, nx), ip = wrapx(i + 1, nx), jm = wrapx(j - 1, ny), jp = wrapx(j + 1, ny);
+  const int row = k * plane;
+  // ---- w point (face k): cbar_w, the w*div term, buoyancy is gathered at cells below
+  {
+    float cw = 0.f, wb = 0.f;
+    const float Rw = LD(a.Rwb, id);
+    if (k >= 1 && k < nz) {
+      const float den = 0.5f * (c.rho[k - 1] + c.rho[k]);
+      cw = Rw / den;
+      wb = Rw * 0.5f * (LD(a.div, id - plane) + LD(a.div, id)) / den;
+    }
+    a.cb[2][id] = cw;
+    a.xsb.w[id] += wb;
+    if (a.sgsb_w && k >= 1 && k < nz) a.sgsb_w[id] += Rw;
+  }
+  if (k >= nz) return;
+  const float r = c.rho[k];
+  // ---- scalars
+  const float Tb = LD(a.Tnb, id), Qb = LD(a.qnb, id);
+  const float cT = a.dts * Tb / r, cQ = a.dts * Qb / r;
+  a.cb[3][id] = cT;
+  a.cb[4][id] = cQ;
+  const float dv = LD(a.div, id);
+  const float T = LD(a.xs.T, id), q = LD(a.xs.q, id);
+  float dvb = cT * T + cQ * q;
+  float Tsb = cT * dv, qsb = cQ * dv;
+  a.x0b.T[id] += Tb;
+  a.x0b.q[id] += Qb;
+  if (a.sgsb_T) {
+    a.sgsb_T[id] += a.dts * Tb;
+    a.sgsb_q[id] += a.dts * Qb;
+  }
+  // ---- u, v points
+  const float Ru = LD(a.Rub, id), Rv = LD(a.Rvb, id);
+  a.cb[0][id] = Ru / r;
+  a.cb[1][id] = Rv / r;
+  float ub = Ru * 0.5f * (LD(a.div, row + j * nx + im) + dv) / r;
+  float vb = Rv * 0.5f * (LD(a.div, row + jm * nx + i) + dv) / r;
+  if (a.sgsb_u) {
+    a.sgsb_u[id] += Ru;
+    a.sgsb_v[id] += Rv;
+  }
+  // divergence adjoint of this cell from the phi*div terms of its u, v, w points
+  dvb += 0.5f / r * (Ru * LD(a.xs.u, id) + LD(a.Rub, row + j * nx + ip) * LD(a.xs.u, row + j * nx + ip));
+  dvb += 0.5f / r * (Rv * LD(a.xs.v, id) + LD(a.Rvb, row + jp * nx + i) * LD(a.xs.v, row + jp * nx + i));
+  if (k >= 1) dvb += 0.5f * LD(a.Rwb, id) * LD(a.xs.w, id) / (0.5f * (c.rho[k - 1] + r));
+  if (k + 1 < nz) dvb += 0.5f * LD(a.Rwb, id + plane) * LD(a.xs.w, id + plane) / (0.5f * (r + c.rho[k + 1]));
+  // Coriolis: R_u += f v4, R_v -= f u4 (both cor_opt 1 and 2 are linear in the winds)
+  if (ph.cor_opt) {
+    const float f4 = 0.25f * ph.f_cor;
+    vb += f4 * (Ru + LD(a.Rub, row + j * nx + ip) + LD(a.Rub, row + jm * nx + i) + LD(a.Rub, row + jm * nx + ip));
+    ub -= f4 * (Rv + LD(a.Rvb, row + jp * nx + i) + LD(a.Rvb, row + j * nx + im) + LD(a.Rvb, row + jp * nx + im));
+  }
+  a.xsb.u[id] += ub;
+  a.xsb.v[id] += vb;
+  a.divb[id] = dvb;
+  // buoyancy b(k) enters b8w on faces k and k+1 (the end faces' extrapolations meet a zero R_w
+  // adjoint: the acoustic sub-step pins w there)
+  {
+    const float bb = 0.5f * ((k >= 1 ? LD(a.Rwb, id) : 0.f) + (k + 1 < nz ? LD(a.Rwb, id + plane) : 0.f));
+    const float th0 = c.theta0[k], q0 = c.qv0[k], tr0 = c.trho0[k];
+    const float reps = (float)kReps;
+    const float num = th0 * (float)(kReps - 1.0) * (q - q0) + (T - c.d0[k]) * (1.f + reps * q) * (1.f + q0);
+    const float den = (1.f + q) * (1.f + q0);
+    const float g = (float)kG / tr0;
+    Tsb += bb * g * (1.f + reps * q) * (1.f + q0) / den;
+    const float dnum = th0 * (float)(kReps - 1.0) + (T - c.d0[k]) * reps * (1.f + q0);
+    qsb += bb * g * (dnum * den - num * (1.f + q0)) / (den * den);
+  }
+  // theta_rho = (theta_ref + T)(1 + reps q)/(1 + q)
+  {
+    const float trb = LD(a.trhob, id);
+    const float reps = (float)kReps;
+    Tsb += trb * (1.f + reps * q) / (1.f + q);
+    qsb += trb * (ph.theta_ref + T) * (reps - 1.f) / ((1.f + q) * (1.f + q));
+  }
+  a.xsb.T[id] += Tsb;
+  a.xsb.q[id] += qsb;
+  a.xsb.p[id] += LD(a.psb, id);
+}
+
+// mass divergence: xsb winds += div^T(divb)
+__global__ void __launch_bounds__(AB) k_massdiv_vjp(Dims d, Phys ph, Cols c, const float* __restrict__ divb, State xsb) {
+  const long long t = (long long)blockIdx.x * AB + threadIdx.x;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
+  if (t >= d.faces()) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
+  const int id = (int)t;
+  if (k >= 1 && k < nz) xsb.w[id] += c.rho_face0[k] * (LD(divb, id - plane) - LD(divb, id)) * ph.rdz;
+  if (k >= nz) return;
+  const float r = c.rho[k];
+  const int row = k * plane;
+  xsb.u[id] += r * (LD(divb, row + j * nx + wrapx(i - 1, nx)) - LD(divb, id)) * ph.rdx;
+  xsb.v[id] += r * (LD(divb, row + wrapx(j - 1, ny) * nx + i) - LD(divb, id)) * ph.rdy;
+}
+
+// ---------------------------------------------------------------------------------------------
+// WENO advection adjoint, one direction
+// ---------------------------------------------------------------------------------------------
+// point p of field f along direction D: neighbour at offset o (wrapped / or -1 outside the column)
+template <int D>
+__device__ __forceinline__ int along(const Dims& d, int i, int j, int k, int o, int n) {
+  if (D == 0) return (k * d.ny + j) * d.nx + wrapx(i + o, d.nx);
+  if (D == 1) return (k * d.ny + wrapx(j + o, d.ny)) * d.nx + i;
+  const int kk = k + o;
+  return (kk < 0 || kk >= n) ? -1 : (kk * d.ny + j) * d.nx + i;
+}
+
+// fields: 0 u, 1 v, 2 w, 3 theta, 4 qv
+template <int D>
+__global__ void __launch_bounds__(AB) k_adv_face_vjp(Dims d, Phys ph, Cols c, AdvVjpArgs a) {
+  const long long t = (long long)blockIdx.x * AB + threadIdx.x;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
+  if (t >= d.faces()) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
+  const int id = (int)t;
+  const float rd = D == 0 ? ph.rdx : (D == 1 ? ph.rdy : ph.rdz);
+  const int im = wrapx(i - 1, nx), jm = wrapx(j - 1, ny);
+  float mbar_s = 0.f;
+  for (int f = 0; f < 5; ++f) {
+    const int n = f == 2 ? nz + 1 : nz;  // points in the field's column
+    const float* phi = a.phi[f];
+    float slots[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float mbar = 0.f;
+    bool valid;
+    if (D < 2)
+      valid = f == 2 ? (k >= 1 && k < nz) : (k < nz);
+    else
+      valid = k >= 1 && k < n;  // face H = k between column entries k-1 and k
+    if (valid) {
+      // mass flux
+      float m;
+      const float r = k < nz ? c.rho[k] : 0.f, rm = k >= 1 ? c.rho[k - 1] : 0.f;
+      if (D == 0) {
+        const float* u = a.xs.u;
+        if (f == 0) m = 0.5f * (LD(u, (k * ny + j) * nx + im) + LD(u, id)) * r;
+        else if (f == 1) m = 0.5f * (r * LD(u, (k * ny + jm) * nx + i) + r * LD(u, id));
+        else if (f == 2) m = 0.5f * (rm * LD(u, id - plane) + r * LD(u, id));
+        else m = r * LD(u, id);
+      } else if (D == 1) {
+        const float* v = a.xs.v;
+        if (f == 0) m = 0.5f * (r * LD(v, (k * ny + j) * nx + im) + r * LD(v, id));
+        else if (f == 1) m = 0.5f * (LD(v, (k * ny + jm) * nx + i) + LD(v, id)) * r;
+        else if (f == 2) m = 0.5f * (rm * LD(v, id - plane) + r * LD(v, id));
+        else m = r * LD(v, id);
+      } else {
+        const float* w = a.xs.w;
+        const float rf = c.rho_face[k];
+        if (f == 0) m = 0.5f * (rf * LD(w, (k * ny + j) * nx + im) + rf * LD(w, id));
+        else if (f == 1) m = 0.5f * (rf * LD(w, (k * ny + jm) * nx + i) + rf * LD(w, id));
+        else if (f == 2) m = 0.5f * (LD(w, id - plane) + LD(w, id)) * rm;
+        else m = rf * LD(w, id);
+      }
+      // flux adjoint: the flux between points p-1 and p leaves p-1 and enters p
+      const int pm = along<D>(d, i, j, k, -1, n);
+      const float Fb = (LD(a.cb[f], id) - LD(a.cb[f], pm)) * rd;
+      float s[6];
+      for (int q = 0; q < 6; ++q) {
+        const int pq = along<D>(d, i, j, k, q - 3, n);
+        s[q] = pq >= 0 ? LD(phi, pq) : 0.f;
+      }
+      const float eps = f < 3 ? kWepsMom : (f == 3 ? kWepsTheta : kWepsQv);
+      float g[6];
+      const float W = D < 2 ? lateral_grad(m, s, eps, g) : vertical_grad(m, s, k, n, eps, g);
+      for (int q = 0; q < 6; ++q) slots[q] = Fb * m * g[q];
+      mbar = Fb * W;
+    }
+    for (int q = 0; q < 6; ++q) a.P[f][q][id] = slots[q];
+    if (f < 3) a.mb[f][id] = mbar;
+    else mbar_s += mbar;
+  }
+  a.mb[3][id] = mbar_s;
+}
+
+template <int D>
+__global__ void __launch_bounds__(AB) k_adv_gather_vjp(Dims d, Phys ph, Cols c, AdvVjpArgs a) {
+  const long long t = (long long)blockIdx.x * AB + threadIdx.x;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
+  if (t >= d.faces()) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
+  const int id = (int)t;
+  float* out[5] = {a.xsb.u, a.xsb.v, a.xsb.w, a.xsb.T, a.xsb.q};
+  for (int f = 0; f < 5; ++f) {
+    const int n = f == 2 ? nz + 1 : nz;
+    if (k >= n) continue;
+    float acc = 0.f;
+    // the flux at point p+3-q names this point in its slot q
+    for (int q = 0; q < 6; ++q) {
+      const int pf = along<D>(d, i, j, k, 3 - q, nz + 1);  // fluxes exist on face levels 0..nz
+      if (pf >= 0) acc += LD(a.P[f][q], pf);
+    }
+    out[f][id] += acc;
+  }
+  // mass-flux adjoints into the wind of direction D
+  const int ip = wrapx(i + 1, nx), jp = wrapx(j + 1, ny);
+  if (D == 0) {
+    if (k >= nz) return;
+    const float r = c.rho[k];
+    const int row = k * plane;
+    float ub = r * LD(a.mb[3], id);                                                     // theta, qv
+    ub += 0.5f * r * (LD(a.mb[0], id) + LD(a.mb[0], row + j * nx + ip));                // u
+    ub += 0.5f * r * (LD(a.mb[1], id) + LD(a.mb[1], row + wrapx(j + 1, ny) * nx + i));  // v (corner)
+    ub += 0.5f * r * ((k >= 1 ? LD(a.mb[2], id) : 0.f) + (k + 1 < nz ? LD(a.mb[2], id + plane) : 0.f));  // w
+    a.xsb.u[id] += ub;
+  } else if (D == 1) {
+    if (k >= nz) return;
+    const float r = c.rho[k];
+    const int row = k * plane;
+    float vb = r * LD(a.mb[3], id);
+    vb += 0.5f * r * (LD(a.mb[0], id) + LD(a.mb[0], row + j * nx + ip));
+    vb += 0.5f * r * (LD(a.mb[1], id) + LD(a.mb[1], row + jp * nx + i));
+    vb += 0.5f * r * ((k >= 1 ? LD(a.mb[2], id) : 0.f) + (k + 1 < nz ? LD(a.mb[2], id + plane) : 0.f));
+    a.xsb.v[id] += vb;
+  } else {
+    const int row = k * plane;
+    float wb = 0.f;
+    if (k >= 1 && k < nz) {
+      const float rf = c.rho_face[k];
+      wb += rf * LD(a.mb[3], id);
+      wb += 0.5f * rf * (LD(a.mb[0], id) + LD(a.mb[0], row + j * nx + ip));
+      wb += 0.5f * rf * (LD(a.mb[1], id) + LD(a.mb[1], row + jp * nx + i));
+    }
+    if (k >= 1) wb += 0.5f * c.rho[k - 1] * LD(a.mb[2], id);
+    if (k + 1 <= nz) wb += 0.5f * c.rho[k] * LD(a.mb[2], id + plane);
+    a.xsb.w[id] += wb;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_acoustic_vjp(const Dims& d, const Phys& ph, const Cols& c, const AcousticVjpArgs& a, float dtau,
+                                cudaStream_t st) {
+  const unsigned g = (unsigned)((d.cells() + AB - 1) / AB);
+  k_acoustic_vjp<<<g, AB, 0, st>>>(d, ph, c, a, dtau);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stage_pointwise_vjp(const Dims& d, const Phys& ph, const Cols& c, const StageVjpArgs& a,
+                                       cudaStream_t st) {
+  const unsigned g = (unsigned)((d.faces() + AB - 1) / AB);
+  k_stage_pointwise_vjp<<<g, AB, 0, st>>>(d, ph, c, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_massdiv_vjp(const Dims& d, const Phys& ph, const Cols& c, const float* divb, State xsb,
+                               cudaStream_t st) {
+  const unsigned g = (unsigned)((d.faces() + AB - 1) / AB);
+  k_massdiv_vjp<<<g, AB, 0, st>>>(d, ph, c, divb, xsb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adv_vjp(const Dims& d, const Phys& ph, const Cols& c, const AdvVjpArgs& a, cudaStream_t st) {
+  const unsigned g = (unsigned)((d.faces() + AB - 1) / AB);
+  k_adv_face_vjp<0><<<g, AB, 0, st>>>(d, ph, c, a);
+  k_adv_gather_vjp<0><<<g, AB, 0, st>>>(d, ph, c, a);
+  k_adv_face_vjp<1><<<g, AB, 0, st>>>(d, ph, c, a);
+  k_adv_gather_vjp<1><<<g, AB, 0, st>>>(d, ph, c, a);
+  k_adv_face_vjp<2><<<g, AB, 0, st>>>(d, ph, c, a);
+  k_adv_gather_vjp<2><<<g, AB, 0, st>>>(d, ph, c, a);
+  return cudaGetLastError();
+}
+
+}  // namespace lexgb
+
+namespace lexgb {
+namespace {
+__global__ void k_axpy(float* __restrict__ y, const float* __restrict__ x, size_t n) {
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    y[t] += x[t];
+}
+}  // namespace
+
+cudaError_t launch_axpy(float* y, const float* x, size_t n, cudaStream_t st) {
+  const unsigned g = (unsigned)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
+  k_axpy<<<g > 0 ? g : 1, 256, 0, st>>>(y, x, n);
+  return cudaGetLastError();
+}
+}  // namespace lexgb

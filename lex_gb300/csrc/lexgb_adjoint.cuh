@@ -1,0 +1,49 @@
+// lexgb_adjoint.cuh - argument blocks and launchers of the reverse-mode (adjoint) kernels.
+#pragma once
+#include "lexgb_internal.cuh"
+
+namespace lexgb {
+
+// One acoustic sub-step backwards: from the adjoint of its output (unb .. pnb) to the adjoint of
+// its input (ub .. pb), accumulating the adjoints of the stage constants.
+struct AcousticVjpArgs {
+  const float *p, *trho, *ps;            // input pi', stage theta_rho and pi'_s
+  const float *un, *vn, *wn;             // output winds of the sub-step
+  const float *unb, *vnb, *wnb, *pnb;    // adjoint of the output
+  float *ub, *vb, *wb, *pb;              // adjoint of the input (written)
+  float *Rub, *Rvb, *Rwb, *trhob, *psb;  // accumulated
+};
+
+// Pointwise part of one stage backwards (after its acoustic loop).
+struct StageVjpArgs {
+  State xs;                                   // stage input state
+  const float* div;                           // its mass divergence
+  const float *Tnb, *qnb;                     // adjoint of the stage's theta / qv outputs
+  const float *Rub, *Rvb, *Rwb, *trhob, *psb; // from the acoustic loop
+  float dts;
+  State xsb;                                  // adjoint of the stage input (accumulated)
+  State x0b;                                  // adjoint of the big step's input (T, q accumulated)
+  float* cb[5];                               // adjoint of the flux convergence per field (u, v, w, T, q)
+  float* divb;                                // adjoint of the mass divergence (written)
+  float *sgsb_u, *sgsb_v, *sgsb_w, *sgsb_T, *sgsb_q;  // SGS tendency adjoints (accumulated; null: off)
+};
+
+// WENO advection backwards for the five advected fields.
+struct AdvVjpArgs {
+  State xs;              // stage input (winds for the mass fluxes)
+  const float* phi[5];   // advected fields u, v, w, T, q
+  const float* cb[5];
+  float* P[5][6];        // per-flux stencil adjoints, slot q = point p-3+q of the flux between p-1, p
+  float* mb[4];          // mass-flux adjoints: u, v, w fluxes and theta+qv fluxes
+  State xsb;             // accumulated
+};
+
+cudaError_t launch_acoustic_vjp(const Dims&, const Phys&, const Cols&, const AcousticVjpArgs&, float dtau,
+                                cudaStream_t);
+cudaError_t launch_stage_pointwise_vjp(const Dims&, const Phys&, const Cols&, const StageVjpArgs&, cudaStream_t);
+cudaError_t launch_massdiv_vjp(const Dims&, const Phys&, const Cols&, const float* divb, State xsb, cudaStream_t);
+cudaError_t launch_adv_vjp(const Dims&, const Phys&, const Cols&, const AdvVjpArgs&, cudaStream_t);
+// y += x over n floats
+cudaError_t launch_axpy(float* y, const float* x, size_t n, cudaStream_t);
+
+}  // namespace lexgb

@@ -162,6 +162,25 @@ class Solver:
     def synchronize(self):
         check(self.lib.lexgb_synchronize(self.handle))
 
+    # -------------------------------------------------------------------------------- reverse mode
+    def step_vjp(self, ybar, nstages=3):
+        """Vector-Jacobian product of one big step (or its first `nstages` stages) at the resident
+        state.  ybar / result: interior arrays in reference order [x][y][z] for (theta, u, v, w,
+        pi', qv), w with nz+1 levels; the result is the adjoint of the resident state."""
+        shapes = [interior_shape(self.nx, self.ny, self.nz, n) for n in FIELDS]
+        shapes[1], shapes[2] = (self.nx, self.ny, self.nz), (self.nx, self.ny, self.nz)   # periodic u, v
+        dev = []
+        for a, shp in zip(ybar, shapes):
+            a = np.asarray(a, dtype=np.float32)
+            if a.shape != shp:
+                raise ValueError("adjoint seed shape %s, expected %s" % (a.shape, shp))
+            dev.append(np.ascontiguousarray(a.transpose(2, 1, 0)))
+        out = [np.empty(shp[::-1], dtype=np.float32) for shp in shapes]
+        yp = (ctypes.c_void_p * 6)(*[a.ctypes.data for a in dev])
+        xp = (ctypes.c_void_p * 6)(*[a.ctypes.data for a in out])
+        check(self.lib.lexgb_step_vjp(self.handle, int(nstages), yp, xp, 0))
+        return tuple(np.ascontiguousarray(a.transpose(2, 1, 0)) for a in out)
+
     # -------------------------------------------------------------------------------- diagnostics
     _DIAG_SHAPES = {"adv_u": "u", "adv_v": "v", "adv_w": "w", "buoy_w": "w", "pgf_u": "u", "pgf_v": "v",
                     "pgf_w": "w", "sgs_u": "u", "sgs_v": "v", "sgs_w": "w"}

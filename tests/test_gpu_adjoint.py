@@ -1,0 +1,103 @@
+"""Reverse mode of the big step (lexgb_step_vjp) against central finite differences of the FP64
+oracle: for random directions v and adjoint seeds ybar,
+
+    <ybar, J v>  (oracle, FP64, (F(x + eps v) - F(x - eps v)) / 2 eps)
+    <J^T ybar, v> (GPU reverse mode, FP32)
+
+must agree to 1e-4 relative to ||ybar|| ||J v||.  Seeds restricted to single output fields
+check the paths one at a time (theta/qv update, acoustic winds, pi')."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, ROOT
+from test_gpu_parity import FIELDS
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+REPORT = {}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def report():
+    yield
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    with open(os.path.join(ROOT, "gpurun_out", "adjoint_report.json"), "w") as f:
+        json.dump(REPORT, f, indent=1, sort_keys=True)
+
+
+def _setup(nstages):
+    from oracle.ic import Grid
+    from oracle.dycore import Dycore
+    from lex_gb300.solver import Solver
+    g = load_golden("ops_random.npz")
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    base = dict(theta0=g["col_theta0"], qv0=g["col_qv0"], pi0=g["col_pi0"], rho0=g["col_rho0"])
+    D = Dycore(Grid(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"])), base, float(g["dt"]),
+               int(g["n_sound"]), turb=False)
+    S = Solver(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"]), float(g["dt"]), int(g["n_sound"]),
+               turb_opt=0)
+    S.set_base_columns(g["col_theta0"], g["col_qv0"], g["col_pi0"], g["col_rho0"])
+    x0 = tuple(g["in_" + f] for f in FIELDS)
+    S.upload(x0)
+
+    def forward(x):
+        if nstages == 3:
+            return D.step(x)[0]
+        xs = x
+        for s, (dts, n) in enumerate(D.stage_plan()[:nstages]):
+            xs, _ = D.stage(x, xs, dts, None, n)
+        return xs
+    return g, D, S, x0, forward
+
+
+def _pad(v):
+    from oracle.ic import pad_scalar, pad_u, pad_v
+    T, u, v_, w, p, q = v
+    return (pad_scalar(T), pad_u(np.concatenate([u, u[:1]], 0)), pad_v(np.concatenate([v_, v_[:, :1]], 1)),
+            pad_scalar(w), pad_scalar(p), pad_scalar(q))
+
+
+def _interior(x, nx, ny):
+    T, u, v, w, p, q = x
+    c = (slice(3, -3), slice(3, -3), slice(1, -1))
+    return (T[c], u[3:3 + nx, 3:-3, 1:-1], v[3:-3, 3:3 + ny, 1:-1], w[c], p[c], q[c])
+
+
+def _direction(rng, nx, ny, nz):
+    w = rng.standard_normal((nx, ny, nz + 1)) * 0.5
+    w[:, :, 0] = 0.0
+    w[:, :, -1] = 0.0
+    return (rng.standard_normal((nx, ny, nz)) * 0.3, rng.standard_normal((nx, ny, nz)), rng.standard_normal((nx, ny, nz)),
+            w, rng.standard_normal((nx, ny, nz)) * 1e-4, rng.standard_normal((nx, ny, nz)) * 1e-4)
+
+
+@pytest.mark.parametrize("nstages,only", [(1, None), (1, "theta"), (1, "pip"), (1, "u"), (1, "w"),
+                                          (3, None)],
+                         ids=["stage0", "stage0_theta", "stage0_pip", "stage0_u", "stage0_w", "step"])
+def test_reverse_mode_matches_oracle_finite_differences(built_lib, nstages, only):
+    g, D, S, x0, forward = _setup(nstages)
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    rng = np.random.default_rng(7)
+    errs = []
+    for trial in range(3):
+        v = _direction(rng, nx, ny, nz)
+        yb = _direction(rng, nx, ny, nz)
+        if only is not None:
+            yb = tuple(a if f == only else np.zeros_like(a) for f, a in zip(FIELDS, yb))
+        eps = 1e-3
+        vp = _pad(v)
+        xp = tuple(a + eps * b for a, b in zip(x0, vp))
+        xm = tuple(a - eps * b for a, b in zip(x0, vp))
+        jv = [(a - b) / (2 * eps) for a, b in zip(_interior(forward(xp), nx, ny), _interior(forward(xm), nx, ny))]
+        lhs = sum(float(np.sum(a * b)) for a, b in zip(yb, jv))
+        xb = S.step_vjp(yb, nstages=nstages)
+        rhs = sum(float(np.sum(np.asarray(a, np.float64) * b)) for a, b in zip(xb, v))
+        scale = np.sqrt(sum(float(np.sum(a * a)) for a in yb)) * np.sqrt(sum(float(np.sum(a * a)) for a in jv))
+        errs.append((lhs, rhs, abs(lhs - rhs) / scale))
+    S.close()
+    REPORT["%d_%s" % (nstages, only)] = errs
+    assert all(e[2] <= TOL for e in errs), errs
