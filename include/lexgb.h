@@ -188,8 +188,8 @@ int lexgb_budget_noalloc(int nx, int ny, int nz, double dx, double dy, double dz
  * w [nz+1][ny][nx] (u on west faces, v on south faces, w on faces 0..nz), FP32, host pointers
  * (on_device = 0) or device pointers (on_device = 1).
  * Replaces jax.vjp of ws_rk3_big_step (one_sprint_functions.py:10-30) as used by the training
- * loop (lex_dl_train.py:114).  Requires turb_opt = 0 (the Smagorinsky terms have no reverse mode
- * yet: LEXGB_ERR_ARG). */
+ * loop (lex_dl_train.py:114).  With turb_opt = 1 the Smagorinsky tendencies, taken from the
+ * step's input state, are differentiated as well. */
 int lexgb_step_vjp(lexgb_ctx *ctx, int nstages, const float *const ybar[6], float *xbar[6], int on_device);
 
 int lexgb_last_error(char *buf, size_t len);

@@ -747,9 +747,11 @@ struct AdjWork {
   float* P[5][6];
   float* mb[4];
   float* sgsb[5];
+  SmagLin sl;
+  SmagVjpArgs sv;
 };
 
-int adj_fields(const StagePlan& p) { return 6 + 15 + 4 * (p.n[0] + p.n[1] + p.n[2]) + 18 + 8 + 5 + 6 + 34 + 5; }
+int adj_fields(const StagePlan& p) { return 6 + 15 + 4 * (p.n[0] + p.n[1] + p.n[2]) + 18 + 8 + 5 + 6 + 34 + 5 + 22; }
 
 int ensure_adjoint(lexgb_ctx* c, AdjWork& w) {
   const StagePlan p = plan_of(c->cfg);
@@ -784,6 +786,14 @@ int ensure_adjoint(lexgb_ctx* c, AdjWork& w) {
   for (int f = 0; f < 5; ++f) for (int s = 0; s < 6; ++s) w.P[f][s] = take();
   for (int f = 0; f < 4; ++f) w.mb[f] = take();
   for (int f = 0; f < 5; ++f) w.sgsb[f] = take();
+  for (int f = 0; f < 6; ++f) w.sl.s[f] = take();
+  w.sl.km = take();
+  w.sl.kS = take();
+  for (int f = 0; f < 6; ++f) w.sv.tb[f] = take();
+  w.sv.khb = take();
+  for (int f = 0; f < 6; ++f) w.sv.sb[f] = take();
+  w.sv.n2b = take();
+  w.sv.gu = w.sgsb[0]; w.sv.gv = w.sgsb[1]; w.sv.gw = w.sgsb[2]; w.sv.gT = w.sgsb[3]; w.sv.gq = w.sgsb[4];
   if ((size_t)(q - c->adj_arena) > nf * c->fstride) return fail(LEXGB_ERR_STATE, "adjoint workspace layout");
   return LEXGB_OK;
 }
@@ -800,21 +810,25 @@ int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float*
   if (nstages < 1 || nstages > 3 || !ybar || !xbar) return fail(LEXGB_ERR_ARG, "need 1..3 stages, ybar and xbar");
   for (int f = 0; f < 6; ++f)
     if (!ybar[f] || !xbar[f]) return fail(LEXGB_ERR_ARG, "null field pointer");
-  if (c->cfg.turb_opt != 0) return fail(LEXGB_ERR_ARG, "reverse mode of the Smagorinsky terms is not built: use turb_opt 0");
   AdjWork w;
   CKS(ensure_adjoint(c, w));
   const Dims& d = c->d;
   const StagePlan p = plan_of(c->cfg);
   const State& A = c->A;
-  const Sgs none{nullptr, nullptr, nullptr, nullptr, nullptr};
+  const bool turb = c->cfg.turb_opt == 1;
+  Sgs sg{nullptr, nullptr, nullptr, nullptr, nullptr};
+  if (turb) {
+    CKS(run_smag(c, A, nullptr, nullptr));
+    sg = Sgs{c->sgs[0], c->sgs[1], c->sgs[2], c->sgs[3], c->sgs[4]};
+  }
   // ---- forward, keeping every intermediate the reverse pass reads
   for (int s = 0; s < nstages; ++s) {
     const State xs = s == 0 ? A : w.S[s];
     const State& out = w.S[s + 1];
     CK(launch_div_trho(d, c->ph, c->cols, xs, w.div[s], w.trho[s], c->stream));
     SlowOut so{nullptr, nullptr, nullptr, out.T, out.q, nullptr, nullptr};
-    CK(launch_adv_scalars(d, c->ph, c->cols, xs, w.div[s], A.T, A.q, none, (float)p.dts[s], so, c->stream));
-    CK(launch_adv_momentum(d, c->ph, c->cols, xs, w.div[s], none, w.Ru[s], w.Rv[s], w.Rw[s], 0, c->stream));
+    CK(launch_adv_scalars(d, c->ph, c->cols, xs, w.div[s], A.T, A.q, sg, (float)p.dts[s], so, c->stream));
+    CK(launch_adv_momentum(d, c->ph, c->cols, xs, w.div[s], sg, w.Ru[s], w.Rv[s], w.Rw[s], 0, c->stream));
     AcousticIn in{A.u, A.v, A.w, A.p, w.Ru[s], w.Rv[s], w.Rw[s], w.trho[s], xs.p};
     for (int m = 1; m <= p.n[s]; ++m) {
       const AcousticOut o{w.ac[s][m][0], w.ac[s][m][1], w.ac[s][m][2], w.ac[s][m][3]};
@@ -831,6 +845,8 @@ int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float*
                        c->stream));
   }
   CKS(zero_state(c, w.Xb0));
+  if (turb)
+    for (int f = 0; f < 5; ++f) CK(cudaMemsetAsync(w.sgsb[f], 0, c->fstride * sizeof(float), c->stream));
   // ---- reverse
   for (int s = nstages - 1; s >= 0; --s) {
     const State xs = s == 0 ? A : w.S[s];
@@ -864,6 +880,9 @@ int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float*
     sa.x0b = w.Xb0;
     for (int f = 0; f < 5; ++f) sa.cb[f] = w.cb[f];
     sa.divb = w.divb;
+    if (turb) {
+      sa.sgsb_u = w.sgsb[0]; sa.sgsb_v = w.sgsb[1]; sa.sgsb_w = w.sgsb[2]; sa.sgsb_T = w.sgsb[3]; sa.sgsb_q = w.sgsb[4];
+    }
     CK(launch_stage_pointwise_vjp(d, c->ph, c->cols, sa, c->stream));
     AdvVjpArgs aa{};
     aa.xs = xs;
@@ -881,6 +900,11 @@ int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float*
     } else {
       std::swap(w.Cur, w.Xs);
     }
+  }
+  // the SGS tendencies were taken from the step's input state
+  if (turb) {
+    w.sv.x0b = w.Xb0;
+    CK(launch_smag_vjp(d, c->ph, c->cols, A, w.sl, w.sv, c->stream));
   }
   for (int f = 0; f < 6; ++f) {
     const size_t n = (f == 3 ? faces : cells) * sizeof(float);

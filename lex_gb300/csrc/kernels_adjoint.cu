@@ -17,6 +17,7 @@
 // mass-flux adjoint Fbar * W.  A gather kernel then adds, for every point, the six slots that
 // name it and the mass-flux adjoints of the fluxes whose mass flux it enters.
 #include "lexgb_adjoint.cuh"
+#include "smag_ops.cuh"
 
 namespace lexgb {
 
@@ -475,6 +476,267 @@ __global__ void __launch_bounds__(AB) k_adv_gather_vjp(Dims d, Phys ph, Cols c, 
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Smagorinsky (turbulence.py:9-111, :298-446) backwards
+// ---------------------------------------------------------------------------------------------
+// weight of the edge value e13 / e23 on w face f in s13 / s23 of cell level k (without rho):
+// corner averages inside, the quadratic end extrapolation in the bottom and top cells
+__device__ __forceinline__ float w_edge(int k, int f, int nz) {
+  if (k == 0) return f == 1 ? 0.5f * 1.875f : (f == 2 ? 0.5f * -1.25f : (f == 3 ? 0.5f * 0.375f : 0.f));
+  if (k == nz - 1) return f == nz - 1 ? 0.5f * 1.875f : (f == nz - 2 ? 0.5f * -1.25f : (f == nz - 3 ? 0.5f * 0.375f : 0.f));
+  return (f == k || f == k + 1) ? 0.25f : 0.f;
+}
+// weight of n2_face(f) in N^2 of cell level k
+__device__ __forceinline__ float w_n2(int k, int f, int nz) {
+  if (k == 0) return f == 1 ? 1.875f : (f == 2 ? -1.25f : (f == 3 ? 0.375f : 0.f));
+  if (k == nz - 1) return f == nz - 1 ? 1.875f : (f == nz - 2 ? -1.25f : (f == nz - 3 ? 0.375f : 0.f));
+  return (f == k || f == k + 1) ? 0.5f : 0.f;
+}
+// the cell levels whose s13 / s23 / N^2 read face f: f-1, f and the two end cells (distinct)
+__device__ __forceinline__ int face_cells(int f, int nz, int* ks) {
+  int n = 0;
+  ks[n++] = f - 1;
+  ks[n++] = f;
+  if (f - 1 != 0 && f != 0) ks[n++] = 0;
+  if (f - 1 != nz - 1 && f != nz - 1) ks[n++] = nz - 1;
+  return n;
+}
+
+// forward quantities of compute_deformation / compute_nm / compute_k at every cell (as k_smag_a)
+__global__ void __launch_bounds__(AB) k_smag_lin(Dims d, Phys ph, Cols c, State s, SmagLin o) {
+  using namespace smag;
+  const long long t = (long long)blockIdx.x * AB + threadIdx.x;
+  if (t >= d.cells()) return;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / d.plane());
+  const int id = (int)t;
+  const float r = c.rho[k];
+  const int ip = wrap(i + 1, nx), jp = wrap(j + 1, ny);
+  const float s11 = r * (LD(s.u, d.at(ip, j, k)) - LD(s.u, id)) * ph.rdx;
+  const float s22 = r * (LD(s.v, d.at(i, jp, k)) - LD(s.v, id)) * ph.rdy;
+  const float s33 = r * (LD(s.w, d.at(i, j, k + 1)) - LD(s.w, id)) * ph.rdz;
+  const float s12 = r * (0.25f * (e12(d, ph, s, i, j, k) + e12(d, ph, s, i + 1, j + 1, k) + e12(d, ph, s, i, j + 1, k) +
+                                  e12(d, ph, s, i + 1, j, k)));
+  float s13 = 0.f, s23 = 0.f, n2 = 0.f;
+  int ks[4];
+  (void)ks;
+  for (int f = 1; f < nz; ++f) {  // sum over the faces with nonzero weight
+    const float we = w_edge(k, f, nz), wn = w_n2(k, f, nz);
+    if (we != 0.f) {
+      s13 += we * (e13(d, ph, s, i, j, f) + e13(d, ph, s, i + 1, j, f));
+      s23 += we * (e23(d, ph, s, i, j, f) + e23(d, ph, s, i, j + 1, f));
+    }
+    if (wn != 0.f) n2 += wn * n2_face(d, ph, s, i, j, f);
+  }
+  s13 *= r;
+  s23 *= r;
+  const float s2 = (2.f * (s11 * s11 + s22 * s22 + s33 * s33) + 4.f * (s12 * s12 + s13 * s13 + s23 * s23)) / (r * r);
+  const float s2n2 = s2 - n2 / (float)kPrandtl;
+  const float km = s2n2 > 0.f ? ph.smag_l2 * sqrtf(s2n2) : 0.f;
+  o.s[0][id] = s11; o.s[1][id] = s22; o.s[2][id] = s33; o.s[3][id] = s12; o.s[4][id] = s13; o.s[5][id] = s23;
+  o.km[id] = km;
+  o.kS[id] = s2n2 > 0.f ? 0.5f * ph.smag_l2 / sqrtf(s2n2) : 0.f;
+}
+
+// adjoint of compute_smag: tau_ij, K_h and the direct theta / qv terms of the scalar diffusion
+__global__ void __launch_bounds__(AB) k_smag_tau_vjp(Dims d, Phys ph, Cols c, State s, SmagLin l, SmagVjpArgs a) {
+  const long long t = (long long)blockIdx.x * AB + threadIdx.x;
+  if (t >= d.cells()) return;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
+  const int id = (int)t;
+  const int im = wrapx(i - 1, nx), ip = wrapx(i + 1, nx), jm = wrapx(j - 1, ny), jp = wrapx(j + 1, ny);
+  const float rdx = ph.rdx, rdy = ph.rdy, rdz = ph.rdz;
+  const float r = c.rho[k];
+  auto at = [&](int ii, int jj, int kk) { return (kk * ny + jj) * nx + ii; };
+  const float* U = a.gu;
+  const float* V = a.gv;
+  const float* W = a.gw;
+  // tau11, tau22, tau33
+  a.tb[0][id] = (LD(U, at(ip, j, k)) - LD(U, id)) * rdx / r;
+  a.tb[1][id] = (LD(V, at(i, jp, k)) - LD(V, id)) * rdy / r;
+  float t33 = 0.f;
+  if (k >= 1) t33 -= LD(W, id) * rdz / c.rho_wext[k];
+  if (k + 1 <= nz - 1) t33 += LD(W, id + plane) * rdz / c.rho_wext[k + 1];
+  a.tb[2][id] = t33;
+  // tau12 through d12v (sgs_u) and d12u (sgs_v)
+  {
+    auto d12v = [&](int cc, int jf) {  // adjoint of (t12(cc,jf) - t12(cc,jf-1)) rdy
+      const int c1 = wrapx(cc + 1, nx), c0 = wrapx(cc, nx), j0 = wrapx(jf, ny), j1 = wrapx(jf - 1, ny);
+      return -0.25f / r * (LD(U, at(c1, j0, k)) + LD(U, at(c0, j1, k)) + LD(U, at(c1, j1, k)) + LD(U, at(c0, j0, k)));
+    };
+    auto d12u = [&](int q, int rr) {  // adjoint of (t12(q,rr) - t12(q-1,rr)) rdx
+      const int q0 = wrapx(q, nx), q1 = wrapx(q - 1, nx), r0 = wrapx(rr, ny), r1 = wrapx(rr + 1, ny);
+      return -0.25f / r * (LD(V, at(q0, r1, k)) + LD(V, at(q1, r0, k)) + LD(V, at(q0, r0, k)) + LD(V, at(q1, r1, k)));
+    };
+    a.tb[3][id] = rdy * (d12v(i, j) - d12v(i, j + 1)) + rdx * (d12u(i, j) - d12u(i + 1, j));
+  }
+  // tau13, tau23: sgs_w (centred lateral differences averaged to faces) and sgs_u / sgs_v
+  {
+    float t13 = 0.f, t23 = 0.f;
+    for (int kf = k; kf <= k + 1; ++kf) {
+      if (kf < 1 || kf > nz - 1) continue;
+      const float cw = -0.5f / c.rho_wext[kf];
+      t13 += cw * (LD(W, at(im, j, kf)) - LD(W, at(ip, j, kf))) / (2.f * ph.dx);
+      t23 += cw * (LD(W, at(i, jm, kf)) - LD(W, at(i, jp, kf))) / (2.f * ph.dy);
+      // d13s(cc, k') = (to_w0(t13(cc), k'+1) - to_w0(t13(cc), k')) rdz enters sgs_u(cc), sgs_u(cc+1)
+      auto d13s = [&](int kk) { return -0.5f / c.rho[kk] * (LD(U, at(ip, j, kk)) + LD(U, at(i, j, kk))); };
+      auto d23s = [&](int kk) { return -0.5f / c.rho[kk] * (LD(V, at(i, jp, kk)) + LD(V, at(i, j, kk))); };
+      t13 += 0.5f * rdz * (d13s(kf - 1) - d13s(kf));
+      t23 += 0.5f * rdz * (d23s(kf - 1) - d23s(kf));
+    }
+    a.tb[4][id] = t13;
+    a.tb[5][id] = t23;
+  }
+  // scalar diffusion of theta and qv: direct terms and K_h
+  {
+    const float khc = LD(l.km, id) / (float)kPrandtl;
+    auto kh = [&](int q) { return LD(l.km, q) / (float)kPrandtl; };
+    const int nb[4] = {at(im, j, k), at(ip, j, k), at(i, jm, k), at(i, jp, k)};
+    float khb = 0.f;
+    for (int fld = 0; fld < 2; ++fld) {
+      const float* A = fld == 0 ? s.T : s.q;
+      const float* G = fld == 0 ? a.gT : a.gq;
+      const float a0 = LD(A, id), g0 = LD(G, id);
+      float ab = 0.f;
+      // x faces i (west) and i+1 (east), y faces j and j+1
+      {
+        const float fw = (g0 - LD(G, nb[0])) * rdx / r, fe = (LD(G, nb[1]) - g0) * rdx / r;
+        const float k8w = 0.5f * (khc + kh(nb[0])), k8e = 0.5f * (kh(nb[1]) + khc);
+        ab += -r * rdx * (fw * k8w - fe * k8e);
+        khb += 0.5f * (fw * (-r * (a0 - LD(A, nb[0])) * rdx) + fe * (-r * (LD(A, nb[1]) - a0) * rdx));
+        const float fs = (g0 - LD(G, nb[2])) * rdy / r, fn = (LD(G, nb[3]) - g0) * rdy / r;
+        const float k8s = 0.5f * (khc + kh(nb[2])), k8n = 0.5f * (kh(nb[3]) + khc);
+        ab += -r * rdy * (fs * k8s - fn * k8n);
+        khb += 0.5f * (fs * (-r * (a0 - LD(A, nb[2])) * rdy) + fn * (-r * (LD(A, nb[3]) - a0) * rdy));
+      }
+      if (k >= 1) {  // bottom face k
+        const float fb = g0 * rdz / r - LD(G, id - plane) * rdz / c.rho[k - 1];
+        const float k8 = 0.5f * (kh(id - plane) + khc);
+        ab += -c.rho_wext[k] * k8 * rdz * fb;
+        khb += 0.5f * fb * (-c.rho_wext[k] * (a0 - LD(A, id - plane)) * rdz);
+      }
+      if (k + 1 <= nz - 1) {  // top face k+1
+        const float ft = LD(G, id + plane) * rdz / c.rho[k + 1] - g0 * rdz / r;
+        const float k8 = 0.5f * (khc + kh(id + plane));
+        ab += c.rho_wext[k + 1] * k8 * rdz * ft;
+        khb += 0.5f * ft * (-c.rho_wext[k + 1] * (LD(A, id + plane) - a0) * rdz);
+      }
+      (fld == 0 ? a.x0b.T : a.x0b.q)[id] += ab;
+    }
+    a.khb[id] = khb;
+  }
+}
+
+// adjoint of compute_k and of the S^2 / N^2 combination: sbar_ij and N^2 bar at every cell
+__global__ void __launch_bounds__(AB) k_smag_s_vjp(Dims d, Cols c, SmagLin l, SmagVjpArgs a) {
+  const long long t = (long long)blockIdx.x * AB + threadIdx.x;
+  if (t >= d.cells()) return;
+  const int id = (int)t, k = (int)(t / d.plane());
+  const float r = c.rho[k], km = LD(l.km, id);
+  float s[6], tb[6];
+  float kmb = LD(a.khb, id) / (float)kPrandtl;
+  for (int q = 0; q < 6; ++q) {
+    s[q] = LD(l.s[q], id);
+    tb[q] = LD(a.tb[q], id);
+    kmb += -2.f * s[q] * tb[q];
+  }
+  const float S2b = kmb * LD(l.kS, id);
+  for (int q = 0; q < 6; ++q) a.sb[q][id] = -2.f * km * tb[q] + S2b * (q < 3 ? 4.f : 8.f) * s[q] / (r * r);
+  a.n2b[id] = -S2b / (float)kPrandtl;
+}
+
+// adjoint of compute_deformation and compute_nm: winds and theta / qv
+__global__ void __launch_bounds__(AB) k_smag_state_vjp(Dims d, Phys ph, Cols c, State s, SmagVjpArgs a) {
+  const long long t = (long long)blockIdx.x * AB + threadIdx.x;
+  if (t >= d.faces()) return;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
+  const int id = (int)t;
+  const float rdx = ph.rdx, rdy = ph.rdy, rdz = ph.rdz;
+  auto at = [&](int ii, int jj, int kk) { return (kk * ny + wrapx(jj, ny)) * nx + wrapx(ii, nx); };
+  // adjoint of e12 at (u point q, v face jf), level kk
+  auto e12b = [&](int q, int jf, int kk) {
+    const float* S = a.sb[3];
+    return 0.25f * c.rho[kk] * (LD(S, at(q, jf, kk)) + LD(S, at(q - 1, jf - 1, kk)) + LD(S, at(q, jf - 1, kk)) +
+                                LD(S, at(q - 1, jf, kk)));
+  };
+  // adjoint of e13 at (u point q, row jj, w face f) / e23 at (column ii, v face jf, w face f)
+  auto e13b = [&](int q, int jj, int f) {
+    if (f < 1 || f > nz - 1) return 0.f;
+    int ks[4];
+    const int n = face_cells(f, nz, ks);
+    float acc = 0.f;
+    for (int m = 0; m < n; ++m) {
+      const int kk = ks[m];
+      if (kk < 0 || kk > nz - 1) continue;
+      const float w = w_edge(kk, f, nz);
+      if (w != 0.f) acc += w * c.rho[kk] * (LD(a.sb[4], at(q - 1, jj, kk)) + LD(a.sb[4], at(q, jj, kk)));
+    }
+    return acc;
+  };
+  auto e23b = [&](int ii, int jf, int f) {
+    if (f < 1 || f > nz - 1) return 0.f;
+    int ks[4];
+    const int n = face_cells(f, nz, ks);
+    float acc = 0.f;
+    for (int m = 0; m < n; ++m) {
+      const int kk = ks[m];
+      if (kk < 0 || kk > nz - 1) continue;
+      const float w = w_edge(kk, f, nz);
+      if (w != 0.f) acc += w * c.rho[kk] * (LD(a.sb[5], at(ii, jf - 1, kk)) + LD(a.sb[5], at(ii, jf, kk)));
+    }
+    return acc;
+  };
+  // ---- w on face k
+  {
+    float wb = 0.f;
+    if (k >= 1) wb += c.rho[k - 1] * rdz * LD(a.sb[2], id - plane);
+    if (k <= nz - 1) wb -= c.rho[k] * rdz * LD(a.sb[2], id);
+    wb += 0.5f * rdx * (e13b(i, j, k) - e13b(i + 1, j, k));
+    wb += 0.5f * rdy * (e23b(i, j, k) - e23b(i, j + 1, k));
+    a.x0b.w[id] += wb;
+  }
+  if (k >= nz) return;
+  const float r = c.rho[k];
+  // ---- u (west face of cell i)
+  {
+    float ub = r * rdx * (LD(a.sb[0], at(i - 1, j, k)) - LD(a.sb[0], id));
+    ub += 0.5f * rdy * (e12b(i, j, k) - e12b(i, j + 1, k));
+    ub += 0.5f * rdz * (e13b(i, j, k) - e13b(i, j, k + 1));
+    a.x0b.u[id] += ub;
+  }
+  // ---- v (south face of cell j)
+  {
+    float vb = r * rdy * (LD(a.sb[1], at(i, j - 1, k)) - LD(a.sb[1], id));
+    vb += 0.5f * rdx * (e12b(i, j, k) - e12b(i + 1, j, k));
+    vb += 0.5f * rdz * (e23b(i, j, k) - e23b(i, j, k + 1));
+    a.x0b.v[id] += vb;
+  }
+  // ---- theta, qv through N^2 = g/dz log(theta_rho_m(f) / theta_rho_m(f-1)) on faces k, k+1
+  {
+    auto n2fb = [&](int f) {
+      if (f < 1 || f > nz - 1) return 0.f;
+      int ks[4];
+      const int n = face_cells(f, nz, ks);
+      float acc = 0.f;
+      for (int m = 0; m < n; ++m) {
+        const int kk = ks[m];
+        if (kk < 0 || kk > nz - 1) continue;
+        const float w = w_n2(kk, f, nz);
+        if (w != 0.f) acc += w * LD(a.n2b, at(i, j, kk));
+      }
+      return acc;
+    };
+    const float T = LD(s.T, id), q = LD(s.q, id);
+    const float r1 = (float)kRepsm1;
+    const float trm = (ph.theta_ref + T) * (1.f + r1 * q);
+    const float trmb = (float)kG * rdz * (n2fb(k) - n2fb(k + 1)) / trm;
+    a.x0b.T[id] += trmb * (1.f + r1 * q);
+    a.x0b.q[id] += trmb * (ph.theta_ref + T) * r1;
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_acoustic_vjp(const Dims& d, const Phys& ph, const Cols& c, const AcousticVjpArgs& a, float dtau,
@@ -495,6 +757,16 @@ cudaError_t launch_massdiv_vjp(const Dims& d, const Phys& ph, const Cols& c, con
                                cudaStream_t st) {
   const unsigned g = (unsigned)((d.faces() + AB - 1) / AB);
   k_massdiv_vjp<<<g, AB, 0, st>>>(d, ph, c, divb, xsb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_smag_vjp(const Dims& d, const Phys& ph, const Cols& c, State x0, const SmagLin& l,
+                            const SmagVjpArgs& a, cudaStream_t st) {
+  const unsigned gc = (unsigned)((d.cells() + AB - 1) / AB), gf = (unsigned)((d.faces() + AB - 1) / AB);
+  k_smag_lin<<<gc, AB, 0, st>>>(d, ph, c, x0, l);
+  k_smag_tau_vjp<<<gc, AB, 0, st>>>(d, ph, c, x0, l, a);
+  k_smag_s_vjp<<<gc, AB, 0, st>>>(d, c, l, a);
+  k_smag_state_vjp<<<gf, AB, 0, st>>>(d, ph, c, x0, a);
   return cudaGetLastError();
 }
 

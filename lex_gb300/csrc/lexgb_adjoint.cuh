@@ -38,6 +38,23 @@ struct AdvVjpArgs {
   State xsb;             // accumulated
 };
 
+// Smagorinsky backwards: forward quantities recomputed at xi0, then the adjoint chain
+struct SmagLin {
+  float* s[6];   // rho S_11, S_22, S_33, S_12, S_13, S_23
+  float* km;     // K_m
+  float* kS;     // dK_m / dS^2 (0 where S^2 - N^2/Pr <= 0)
+};
+struct SmagVjpArgs {
+  const float *gu, *gv, *gw, *gT, *gq;  // adjoints of the five SGS tendencies
+  float* tb[6];                         // adjoint of tau_ij
+  float* khb;                           // adjoint of K_h
+  float* sb[6];                         // adjoint of rho S_ij
+  float* n2b;                           // adjoint of N^2
+  State x0b;                            // accumulated adjoint of the state
+};
+cudaError_t launch_smag_vjp(const Dims&, const Phys&, const Cols&, State x0, const SmagLin&, const SmagVjpArgs&,
+                            cudaStream_t);
+
 cudaError_t launch_acoustic_vjp(const Dims&, const Phys&, const Cols&, const AcousticVjpArgs&, float dtau,
                                 cudaStream_t);
 cudaError_t launch_stage_pointwise_vjp(const Dims&, const Phys&, const Cols&, const StageVjpArgs&, cudaStream_t);

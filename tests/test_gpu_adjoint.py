@@ -29,7 +29,7 @@ def report():
         json.dump(REPORT, f, indent=1, sort_keys=True)
 
 
-def _setup(nstages):
+def _setup(nstages, turb=0):
     from oracle.ic import Grid
     from oracle.dycore import Dycore
     from lex_gb300.solver import Solver
@@ -37,9 +37,9 @@ def _setup(nstages):
     nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
     base = dict(theta0=g["col_theta0"], qv0=g["col_qv0"], pi0=g["col_pi0"], rho0=g["col_rho0"])
     D = Dycore(Grid(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"])), base, float(g["dt"]),
-               int(g["n_sound"]), turb=False)
+               int(g["n_sound"]), turb=bool(turb))
     S = Solver(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"]), float(g["dt"]), int(g["n_sound"]),
-               turb_opt=0)
+               turb_opt=turb)
     S.set_base_columns(g["col_theta0"], g["col_qv0"], g["col_pi0"], g["col_rho0"])
     x0 = tuple(g["in_" + f] for f in FIELDS)
     S.upload(x0)
@@ -48,8 +48,9 @@ def _setup(nstages):
         if nstages == 3:
             return D.step(x)[0]
         xs = x
+        sgs = D.smagorinsky(x[0], x[1], x[2], x[3], x[5]) if turb else None
         for s, (dts, n) in enumerate(D.stage_plan()[:nstages]):
-            xs, _ = D.stage(x, xs, dts, None, n)
+            xs, _ = D.stage(x, xs, dts, sgs, n)
         return xs
     return g, D, S, x0, forward
 
@@ -75,11 +76,15 @@ def _direction(rng, nx, ny, nz):
             w, rng.standard_normal((nx, ny, nz)) * 1e-4, rng.standard_normal((nx, ny, nz)) * 1e-4)
 
 
-@pytest.mark.parametrize("nstages,only", [(1, None), (1, "theta"), (1, "pip"), (1, "u"), (1, "w"),
-                                          (3, None)],
-                         ids=["stage0", "stage0_theta", "stage0_pip", "stage0_u", "stage0_w", "step"])
-def test_reverse_mode_matches_oracle_finite_differences(built_lib, nstages, only):
-    g, D, S, x0, forward = _setup(nstages)
+CASES = [(1, None, 0), (1, "theta", 0), (1, "pip", 0), (1, "u", 0), (1, "w", 0), (3, None, 0),
+         (1, None, 1), (1, "theta", 1), (1, "u", 1), (1, "w", 1), (3, None, 1)]
+
+
+@pytest.mark.parametrize("nstages,only,turb", CASES,
+                         ids=["%s%s%s" % ("step" if n == 3 else "stage0", "_" + o if o else "", "_smag" if t else "")
+                              for n, o, t in CASES])
+def test_reverse_mode_matches_oracle_finite_differences(built_lib, nstages, only, turb):
+    g, D, S, x0, forward = _setup(nstages, turb)
     nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
     rng = np.random.default_rng(7)
     errs = []
@@ -99,5 +104,5 @@ def test_reverse_mode_matches_oracle_finite_differences(built_lib, nstages, only
         scale = np.sqrt(sum(float(np.sum(a * a)) for a in yb)) * np.sqrt(sum(float(np.sum(a * a)) for a in jv))
         errs.append((lhs, rhs, abs(lhs - rhs) / scale))
     S.close()
-    REPORT["%d_%s" % (nstages, only)] = errs
+    REPORT["%d_%s_%d" % (nstages, only, turb)] = errs
     assert all(e[2] <= TOL for e in errs), errs
