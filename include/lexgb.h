@@ -178,6 +178,14 @@ int lexgb_budget_noalloc(int nx, int ny, int nz, double dx, double dy, double dz
                          double *out, void *stream);
 
 /* Message of the last failure on this thread; returns the untruncated length. */
+/* The prognostic state in the device layout: interior only, x fastest; theta (K), u, v, pi', qv
+ * [nz][ny][nx] and w [nz+1][ny][nx], FP32, host (on_device = 0) or device pointers (1, e.g. torch
+ * CUDA tensors; ordered on the context's stream).  set marks the state as present.
+ * The device-pointer form of lexgb_upload_state / lexgb_download_state (no reference counterpart:
+ * LEX hands JAX arrays around, one_sprint_functions.py:10-30). */
+int lexgb_set_state_interior(lexgb_ctx *ctx, const float *const fields[6], int on_device);
+int lexgb_get_state_interior(lexgb_ctx *ctx, float *fields[6], int on_device);
+
 /* Reverse mode (vector-Jacobian product) of the first `nstages` (1..3) WS-RK3 stages of one big
  * step taken from the resident state: given ybar, the adjoint of the state after those stages,
  * writes xbar, the adjoint of the resident state.  The resident state is not modified.  The

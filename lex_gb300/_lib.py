@@ -54,6 +54,8 @@ SIGNATURES = {
     "lexgb_time_kernel": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_float)]),
     "lexgb_budget_noalloc": (_I, [_I, _I, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.POINTER(_P), _P, _P, _P, _P]),
+    "lexgb_set_state_interior": (_I, [_P, ctypes.POINTER(_P), _I]),
+    "lexgb_get_state_interior": (_I, [_P, ctypes.POINTER(_P), _I]),
     "lexgb_step_vjp": (_I, [_P, _I, ctypes.POINTER(_P), ctypes.POINTER(_P), _I]),
     "lexgb_last_error": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
 }

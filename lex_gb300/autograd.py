@@ -1,0 +1,95 @@
+"""The big step as a differentiable PyTorch operation on CUDA tensors.
+
+``step(solver, state)`` advances one WS-RK3 big step (one_sprint_functions.py:10-30) and
+records it for autograd; its backward is the hand-written reverse mode of the library
+(``lexgb_step_vjp``).  Only the step's input state is saved (step-level checkpointing): the
+backward pass recomputes the step's stages and acoustic sub-steps from it, so a rollout of N
+steps keeps N states alive, not N times the ~50 intermediate fields of a step.  This replaces
+``jax.vjp`` / ``jax.grad`` through ``ws_rk3_sprint_dl_train`` (one_sprint_functions.py:33-96,
+lex_dl_train.py:114).
+
+State layout: a tuple of six float32 CUDA tensors in the device layout, x fastest -
+theta [K], u, v, pi', qv of shape (nz, ny, nx) and w of shape (nz+1, ny, nx) (u on west faces,
+v on south faces, w on faces 0..nz).  There is no CPU path: without a GPU and the built
+library the calls raise.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from .solver import Solver
+
+
+def _shapes(solver):
+    nx, ny, nz = solver.nx, solver.ny, solver.nz
+    c = (nz, ny, nx)
+    return (c, c, c, (nz + 1, ny, nx), c, c)
+
+
+def _check(solver, tensors):
+    if len(tensors) != 6:
+        raise ValueError("state must have 6 tensors (theta, u, v, w, pi', qv)")
+    for t, shp in zip(tensors, _shapes(solver)):
+        if not t.is_cuda or t.dtype != torch.float32 or tuple(t.shape) != shp:
+            raise ValueError("state tensors must be float32 CUDA tensors of shapes %s" % (_shapes(solver),))
+
+
+def _ptrs(tensors):
+    return (ctypes.c_void_p * 6)(*[t.data_ptr() for t in tensors])
+
+
+def _bind_stream(solver):
+    solver.set_stream(torch.cuda.current_stream().cuda_stream)
+
+
+def set_state(solver, tensors):
+    """Copy a device-layout state into the solver (ordered on torch's current stream)."""
+    tensors = tuple(t.contiguous() for t in tensors)
+    _check(solver, tensors)
+    _bind_stream(solver)
+    _lib.check(solver.lib.lexgb_set_state_interior(solver.handle, _ptrs(tensors), 1))
+
+
+def get_state(solver):
+    """The solver's state as new device-layout tensors."""
+    out = tuple(torch.empty(s, dtype=torch.float32, device="cuda") for s in _shapes(solver))
+    _bind_stream(solver)
+    _lib.check(solver.lib.lexgb_get_state_interior(solver.handle, _ptrs(out), 1))
+    return out
+
+
+class _Step(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, solver, *state):
+        set_state(solver, state)
+        solver.step(1)
+        ctx.solver = solver
+        ctx.save_for_backward(*state)
+        return get_state(solver)
+
+    @staticmethod
+    def backward(ctx, *grads):
+        solver = ctx.solver
+        x = ctx.saved_tensors
+        set_state(solver, x)
+        gy = tuple((g if g is not None else torch.zeros(s, device="cuda")).contiguous().float()
+                   for g, s in zip(grads, _shapes(solver)))
+        gx = tuple(torch.empty(s, dtype=torch.float32, device="cuda") for s in _shapes(solver))
+        _bind_stream(solver)
+        _lib.check(solver.lib.lexgb_step_vjp(solver.handle, 3, _ptrs(gy), _ptrs(gx), 1))
+        return (None,) + gx
+
+
+def step(solver, state):
+    """One differentiable big step: state -> next state (tuples of six CUDA tensors)."""
+    if not isinstance(solver, Solver):
+        raise TypeError("solver must be a lex_gb300.solver.Solver")
+    return _Step.apply(solver, *state)
+
+
+def rollout(solver, state, nsteps):
+    """nsteps differentiable big steps (the sprint of one_sprint_functions.py:109-115)."""
+    for _ in range(int(nsteps)):
+        state = step(solver, state)
+    return state

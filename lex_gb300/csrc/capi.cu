@@ -731,6 +731,46 @@ int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
 }
 
 // ------------------------------------------------------------------------------------------------
+// state in the device layout (interior only, x fastest), theta in K
+// ------------------------------------------------------------------------------------------------
+int lexgb_set_state_interior(lexgb_ctx* c, const float* const fields[6], int on_device) {
+  if (!c || !fields) return fail(LEXGB_ERR_ARG, "null argument");
+  if (!c->base_set) return fail(LEXGB_ERR_STATE, "base state not set");
+  for (int f = 0; f < NFIELD; ++f) {
+    if (!fields[f]) return fail(LEXGB_ERR_ARG, "null field pointer");
+    const size_t n = (f == 3 ? c->d.faces() : c->d.cells()) * sizeof(float);
+    CK(cudaMemcpyAsync(field_of(c->A, f), fields[f], n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                       c->stream));
+  }
+  CK(launch_shift(c->A.T, -(float)c->theta_ref, (size_t)c->d.cells(), c->stream));
+  c->state_set = true;
+  if (!on_device) CK(cudaStreamSynchronize(c->stream));
+  return LEXGB_OK;
+}
+
+int lexgb_get_state_interior(lexgb_ctx* c, float* fields[6], int on_device) {
+  CKS(check_ready(c));
+  if (!fields) return fail(LEXGB_ERR_ARG, "null argument");
+  for (int f = 0; f < NFIELD; ++f) {
+    if (!fields[f]) return fail(LEXGB_ERR_ARG, "null field pointer");
+    const size_t n = (f == 3 ? c->d.faces() : c->d.cells()) * sizeof(float);
+    if (f == 0 && on_device) {
+      CK(cudaMemcpyAsync(fields[0], c->A.T, n, cudaMemcpyDeviceToDevice, c->stream));
+      CK(launch_shift(fields[0], (float)c->theta_ref, (size_t)c->d.cells(), c->stream));
+      continue;
+    }
+    CK(cudaMemcpyAsync(fields[f], field_of(c->A, f), n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                       c->stream));
+  }
+  if (!on_device) {
+    CK(cudaStreamSynchronize(c->stream));
+    const size_t n = (size_t)c->d.cells();
+    for (size_t t = 0; t < n; ++t) fields[0][t] += (float)c->theta_ref;
+  }
+  return LEXGB_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
 // reverse mode
 // ------------------------------------------------------------------------------------------------
 namespace {

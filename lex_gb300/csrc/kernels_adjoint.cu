@@ -797,3 +797,18 @@ cudaError_t launch_axpy(float* y, const float* x, size_t n, cudaStream_t st) {
   return cudaGetLastError();
 }
 }  // namespace lexgb
+
+namespace lexgb {
+namespace {
+__global__ void k_shift(float* __restrict__ y, float c, size_t n) {
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    y[t] += c;
+}
+}  // namespace
+
+cudaError_t launch_shift(float* y, float c, size_t n, cudaStream_t st) {
+  const unsigned g = (unsigned)((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
+  k_shift<<<g > 0 ? g : 1, 256, 0, st>>>(y, c, n);
+  return cudaGetLastError();
+}
+}  // namespace lexgb

@@ -62,5 +62,7 @@ cudaError_t launch_massdiv_vjp(const Dims&, const Phys&, const Cols&, const floa
 cudaError_t launch_adv_vjp(const Dims&, const Phys&, const Cols&, const AdvVjpArgs&, cudaStream_t);
 // y += x over n floats
 cudaError_t launch_axpy(float* y, const float* x, size_t n, cudaStream_t);
+// y += c over n floats
+cudaError_t launch_shift(float* y, float c, size_t n, cudaStream_t);
 
 }  // namespace lexgb
