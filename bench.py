@@ -274,6 +274,56 @@ def run_lexgb(args):
         with open(tp) as f:
             t = json.load(f)
         traffic = t["bytes_per_point"] * npts
+    # ---- reverse mode: one big step forward plus its vector-Jacobian product, device pointers
+    adjoint = None
+    if not args.no_adjoint:
+        import ctypes
+        from lex_gb300 import _lib
+        shp = [(g["nz"], g["ny"], g["nx"])] * 6
+        shp[3] = (g["nz"] + 1, g["ny"], g["nx"])
+        gen = torch.Generator(device="cuda").manual_seed(1)
+        ybar = [torch.randn(sh, device="cuda", generator=gen) for sh in shp]
+        xbar = [torch.empty(sh, device="cuda") for sh in shp]
+        yp = (ctypes.c_void_p * 6)(*[t.data_ptr() for t in ybar])
+        xp = (ctypes.c_void_p * 6)(*[t.data_ptr() for t in xbar])
+        S.upload(phys, dtype=np.float32)
+        torch.cuda.synchronize()
+        _lib.check(S.lib.lexgb_step_vjp(S.handle, 3, yp, xp, 1))   # allocates the workspace
+        reps = 3
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a0.record()
+            for _ in range(reps):
+                _lib.check(S.lib.lexgb_step_vjp(S.handle, 3, yp, xp, 1))
+            a1.record()
+        a1.synchronize()
+        vjp_ms = a0.elapsed_time(a1) / reps
+        # non-checkpointed: the forward keeps its intermediates, the reverse reuses them
+        S.upload(phys, dtype=np.float32)
+        torch.cuda.synchronize()
+        k0 = torch.cuda.Event(enable_timing=True)
+        k1 = torch.cuda.Event(enable_timing=True)
+        k2 = torch.cuda.Event(enable_timing=True)
+        keep_ms = kept_ms = 0.0
+        for _ in range(reps):
+            with torch.cuda.stream(stream):
+                k0.record()
+                _lib.check(S.lib.lexgb_step_keep(S.handle))
+                k1.record()
+                _lib.check(S.lib.lexgb_step_vjp_kept(S.handle, yp, xp, 1))
+                k2.record()
+            k2.synchronize()
+            keep_ms += k0.elapsed_time(k1) / reps
+            kept_ms += k1.elapsed_time(k2) / reps
+        adjoint = {"forward_ms": ms_per_step,
+                   "kept_forward_ms": keep_ms, "kept_reverse_ms": kept_ms,
+                   "forward_plus_adjoint_over_forward": (keep_ms + kept_ms) / ms_per_step,
+                   "checkpointed_reverse_ms": vjp_ms,
+                   "checkpointed_forward_plus_adjoint_over_forward": (ms_per_step + vjp_ms) / ms_per_step,
+                   "note": "forward_plus_adjoint: lexgb_step_keep + lexgb_step_vjp_kept (intermediates kept by "
+                           "the forward); checkpointed: graph forward + lexgb_step_vjp, which recomputes the "
+                           "step; xbar finite: %s" % bool(all(torch.isfinite(t).all().item() for t in xbar))}
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -301,6 +351,8 @@ def run_lexgb(args):
         "nonfinite_after": n_bad,
         "clocks": clk,
     }
+    if adjoint is not None:
+        line["adjoint"] = adjoint
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line), flush=True)
@@ -316,6 +368,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="lexgb", choices=["lexgb", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint cost measurement")
     ap.add_argument("--profile", action="store_true", help="only warm-up + timed steps (profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "lexgb":

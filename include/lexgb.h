@@ -200,6 +200,14 @@ int lexgb_get_state_interior(lexgb_ctx *ctx, float *fields[6], int on_device);
  * step's input state, are differentiated as well. */
 int lexgb_step_vjp(lexgb_ctx *ctx, int nstages, const float *const ybar[6], float *xbar[6], int on_device);
 
+/* One big step that keeps what its reverse mode reads: the resident state advances one step as
+ * with lexgb_step(ctx, 1, 0), and the step's input state and all of its intermediates stay in the
+ * adjoint workspace.  lexgb_step_vjp_kept then returns the adjoint of that input without
+ * recomputing the step (LEXGB_ERR_STATE if there is no kept step: lexgb_step_vjp and a new base
+ * state discard it).  Together they are the non-checkpointed forward + reverse of training. */
+int lexgb_step_keep(lexgb_ctx *ctx);
+int lexgb_step_vjp_kept(lexgb_ctx *ctx, const float *const ybar[6], float *xbar[6], int on_device);
+
 int lexgb_last_error(char *buf, size_t len);
 
 #ifdef __cplusplus

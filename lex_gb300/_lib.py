@@ -57,6 +57,8 @@ SIGNATURES = {
     "lexgb_set_state_interior": (_I, [_P, ctypes.POINTER(_P), _I]),
     "lexgb_get_state_interior": (_I, [_P, ctypes.POINTER(_P), _I]),
     "lexgb_step_vjp": (_I, [_P, _I, ctypes.POINTER(_P), ctypes.POINTER(_P), _I]),
+    "lexgb_step_keep": (_I, [_P]),
+    "lexgb_step_vjp_kept": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), _I]),
     "lexgb_last_error": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
 }
 

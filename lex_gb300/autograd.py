@@ -6,7 +6,9 @@ records it for autograd; its backward is the hand-written reverse mode of the li
 backward pass recomputes the step's stages and acoustic sub-steps from it, so a rollout of N
 steps keeps N states alive, not N times the ~50 intermediate fields of a step.  This replaces
 ``jax.vjp`` / ``jax.grad`` through ``ws_rk3_sprint_dl_train`` (one_sprint_functions.py:33-96,
-lex_dl_train.py:114).
+lex_dl_train.py:114).  The forward keeps the intermediates of the step it ran last
+(``lexgb_step_keep``), so the backward of the most recent step reuses them instead of
+recomputing (``lexgb_step_vjp_kept``); earlier steps of a rollout are recomputed.
 
 State layout: a tuple of six float32 CUDA tensors in the device layout, x fastest -
 theta [K], u, v, pi', qv of shape (nz, ny, nx) and w of shape (nz+1, ny, nx) (u on west faces,
@@ -63,7 +65,10 @@ class _Step(torch.autograd.Function):
     @staticmethod
     def forward(ctx, solver, *state):
         set_state(solver, state)
-        solver.step(1)
+        _bind_stream(solver)
+        _lib.check(solver.lib.lexgb_step_keep(solver.handle))
+        solver._kept_token = getattr(solver, "_kept_token", 0) + 1
+        ctx.token = solver._kept_token
         ctx.solver = solver
         ctx.save_for_backward(*state)
         return get_state(solver)
@@ -71,13 +76,16 @@ class _Step(torch.autograd.Function):
     @staticmethod
     def backward(ctx, *grads):
         solver = ctx.solver
-        x = ctx.saved_tensors
-        set_state(solver, x)
         gy = tuple((g if g is not None else torch.zeros(s, device="cuda")).contiguous().float()
                    for g, s in zip(grads, _shapes(solver)))
         gx = tuple(torch.empty(s, dtype=torch.float32, device="cuda") for s in _shapes(solver))
         _bind_stream(solver)
-        _lib.check(solver.lib.lexgb_step_vjp(solver.handle, 3, _ptrs(gy), _ptrs(gx), 1))
+        if getattr(solver, "_kept_token", None) == ctx.token:   # this step's intermediates are still kept
+            _lib.check(solver.lib.lexgb_step_vjp_kept(solver.handle, _ptrs(gy), _ptrs(gx), 1))
+        else:                                                   # recompute from the saved input
+            set_state(solver, ctx.saved_tensors)
+            _lib.check(solver.lib.lexgb_step_vjp(solver.handle, 3, _ptrs(gy), _ptrs(gx), 1))
+        solver._kept_token = None
         return (None,) + gx
 
 

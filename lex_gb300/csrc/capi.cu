@@ -83,6 +83,7 @@ struct lexgb_ctx {
   unsigned long long* count = nullptr;
   // reverse mode: workspace of the recomputed step and the adjoint fields (allocated on first use)
   float* adj_arena = nullptr;
+  bool adj_kept = false;  // the workspace holds a step kept by lexgb_step_keep
   // graph of one big step
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -264,6 +265,7 @@ int build_table(lexgb_ctx* c) {
   float* t = c->tab;
   c->cols = Cols{t, t + S, t + 2 * S, t + 3 * S, t + 4 * S, t + 5 * S, t + 6 * S, t + 7 * S, t + 8 * S, t + 9 * S};
   c->base_set = true;
+  c->adj_kept = false;
   drop_graph(c);
   return LEXGB_OK;
 }
@@ -780,6 +782,7 @@ struct AdjWork {
   float *div[3], *trho[3], *Ru[3], *Rv[3], *Rw[3];
   float* ac[3][64][4];   // acoustic states 1..n of each stage: u, v, w, p
   State Xb0, Cur, Xs;    // adjoints: step input, current stage output, current stage input
+  State X0;              // input state of a kept step (lexgb_step_keep)
   float* pp[2][4];       // acoustic adjoint ping-pong
   float *Rub, *Rvb, *Rwb, *trhob, *psb;
   float* cb[5];
@@ -791,7 +794,7 @@ struct AdjWork {
   SmagVjpArgs sv;
 };
 
-int adj_fields(const StagePlan& p) { return 6 + 15 + 4 * (p.n[0] + p.n[1] + p.n[2]) + 18 + 8 + 5 + 6 + 34 + 5 + 22; }
+int adj_fields(const StagePlan& p) { return 6 + 15 + 4 * (p.n[0] + p.n[1] + p.n[2]) + 18 + 8 + 5 + 6 + 34 + 5 + 22 + 6; }
 
 int ensure_adjoint(lexgb_ctx* c, AdjWork& w) {
   const StagePlan p = plan_of(c->cfg);
@@ -819,6 +822,7 @@ int ensure_adjoint(lexgb_ctx* c, AdjWork& w) {
   w.Xb0 = fields_at(take(), c->fstride); for (int i = 1; i < NFIELD; ++i) take();
   w.Cur = fields_at(take(), c->fstride); for (int i = 1; i < NFIELD; ++i) take();
   w.Xs = fields_at(take(), c->fstride); for (int i = 1; i < NFIELD; ++i) take();
+  w.X0 = fields_at(take(), c->fstride); for (int i = 1; i < NFIELD; ++i) take();
   for (int a = 0; a < 2; ++a) for (int f = 0; f < 4; ++f) w.pp[a][f] = take();
   w.Rub = take(); w.Rvb = take(); w.Rwb = take(); w.trhob = take(); w.psb = take();
   for (int f = 0; f < 5; ++f) w.cb[f] = take();
@@ -845,23 +849,18 @@ int zero_state(lexgb_ctx* c, const State& s) {
 
 }  // namespace
 
-int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float* xbar[6], int on_device) {
-  CKS(check_ready(c));
-  if (nstages < 1 || nstages > 3 || !ybar || !xbar) return fail(LEXGB_ERR_ARG, "need 1..3 stages, ybar and xbar");
-  for (int f = 0; f < 6; ++f)
-    if (!ybar[f] || !xbar[f]) return fail(LEXGB_ERR_ARG, "null field pointer");
-  AdjWork w;
-  CKS(ensure_adjoint(c, w));
+namespace {
+
+// forward of the first nstages stages from x0, keeping every intermediate the reverse pass reads
+int adj_forward(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages) {
   const Dims& d = c->d;
   const StagePlan p = plan_of(c->cfg);
-  const State& A = c->A;
-  const bool turb = c->cfg.turb_opt == 1;
+  const State& A = x0;
   Sgs sg{nullptr, nullptr, nullptr, nullptr, nullptr};
-  if (turb) {
+  if (c->cfg.turb_opt == 1) {
     CKS(run_smag(c, A, nullptr, nullptr));
     sg = Sgs{c->sgs[0], c->sgs[1], c->sgs[2], c->sgs[3], c->sgs[4]};
   }
-  // ---- forward, keeping every intermediate the reverse pass reads
   for (int s = 0; s < nstages; ++s) {
     const State xs = s == 0 ? A : w.S[s];
     const State& out = w.S[s + 1];
@@ -876,6 +875,16 @@ int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float*
       in.u = o.u; in.v = o.v; in.w = o.w; in.p = o.p;
     }
   }
+  return LEXGB_OK;
+}
+
+// reverse pass over the intermediates adj_forward kept for x0
+int adj_reverse(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages, const float* const ybar[6], float* xbar[6],
+                int on_device) {
+  const Dims& d = c->d;
+  const StagePlan p = plan_of(c->cfg);
+  const State& A = x0;
+  const bool turb = c->cfg.turb_opt == 1;
   // ---- seed
   const size_t cells = (size_t)d.cells(), faces = (size_t)d.faces();
   for (int f = 0; f < 6; ++f) {
@@ -953,6 +962,50 @@ int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float*
   }
   CK(cudaStreamSynchronize(c->stream));
   return LEXGB_OK;
+}
+
+int check_vjp_args(const float* const ybar[6], float* xbar[6]) {
+  if (!ybar || !xbar) return fail(LEXGB_ERR_ARG, "need ybar and xbar");
+  for (int f = 0; f < 6; ++f)
+    if (!ybar[f] || !xbar[f]) return fail(LEXGB_ERR_ARG, "null field pointer");
+  return LEXGB_OK;
+}
+
+}  // namespace
+
+int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float* xbar[6], int on_device) {
+  CKS(check_ready(c));
+  if (nstages < 1 || nstages > 3) return fail(LEXGB_ERR_ARG, "need 1..3 stages");
+  CKS(check_vjp_args(ybar, xbar));
+  AdjWork w;
+  CKS(ensure_adjoint(c, w));
+  c->adj_kept = false;  // the workspace is reused below
+  CKS(adj_forward(c, w, c->A, nstages));
+  return adj_reverse(c, w, c->A, nstages, ybar, xbar, on_device);
+}
+
+int lexgb_step_keep(lexgb_ctx* c) {
+  CKS(check_ready(c));
+  AdjWork w;
+  CKS(ensure_adjoint(c, w));
+  for (int f = 0; f < NFIELD; ++f)
+    CK(cudaMemcpyAsync(field_of(w.X0, f), field_of(c->A, f), c->fstride * sizeof(float), cudaMemcpyDeviceToDevice,
+                       c->stream));
+  CKS(adj_forward(c, w, w.X0, 3));
+  for (int f = 0; f < NFIELD; ++f)
+    CK(cudaMemcpyAsync(field_of(c->A, f), field_of(w.S[3], f), c->fstride * sizeof(float), cudaMemcpyDeviceToDevice,
+                       c->stream));
+  c->adj_kept = true;
+  return LEXGB_OK;
+}
+
+int lexgb_step_vjp_kept(lexgb_ctx* c, const float* const ybar[6], float* xbar[6], int on_device) {
+  CKS(check_ready(c));
+  CKS(check_vjp_args(ybar, xbar));
+  if (!c->adj_kept) return fail(LEXGB_ERR_STATE, "no kept step: call lexgb_step_keep first");
+  AdjWork w;
+  CKS(ensure_adjoint(c, w));
+  return adj_reverse(c, w, w.X0, 3, ybar, xbar, on_device);
 }
 
 int lexgb_last_error(char* buf, size_t len) {

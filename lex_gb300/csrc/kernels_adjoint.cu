@@ -153,90 +153,226 @@ __device__ __forceinline__ float vertical_grad(float m, const float* s, int H, i
 // ---------------------------------------------------------------------------------------------
 // acoustic sub-step
 // ---------------------------------------------------------------------------------------------
+// Values one cell's reverse sub-step reads; neighbour index 0 cell, 1 west, 2 east, 3 south,
+// 4 north, 5 below, 6 above.
+struct AcNbr {
+  float A[7];    // kDivDamp * dtau * adjoint of the output pi'
+  float s[7];    // pi'_s
+  float p[7];    // input pi'
+  float t[7];    // theta_rho
+  float unb_w, unb_e, vnb_s, vnb_n, wnb_b, wnb_t;  // adjoints of the output winds on the six faces
+  float un_w, un_e, vn_s, vn_n, wn_b, wn_t;        // output winds on the six faces
+};
+struct AcCol {  // column constants of level k
+  float pi0m, pi0, pi0p, rhom, rho, rhop, rfb, rft, dzb, dzt;
+  bool hb, ht;
+};
+struct AcOut {
+  float ub, vb, wb, pb, tb, sb;
+};
+
+__device__ __forceinline__ AcOut acoustic_vjp_cell(const AcNbr& n, const AcCol& k, float pnb0, float rdx, float rdy,
+                                                   float rdz, float dtau) {
+  const float* A = n.A;
+  const float* s = n.s;
+  auto divb = [&](int q, float pi0) { return -A[q] * kRdCvA * (pi0 + s[q]); };
+  const float D0 = divb(0, k.pi0), DW = divb(1, k.pi0), DE = divb(2, k.pi0), DS = divb(3, k.pi0), DN = divb(4, k.pi0);
+  const float DB = k.hb ? divb(5, k.pi0m) : 0.f, DT = k.ht ? divb(6, k.pi0p) : 0.f;
+  const float Gw = (s[0] - s[1]) * rdx, Ge = (s[2] - s[0]) * rdx, Gs = (s[0] - s[3]) * rdy, Gn = (s[4] - s[0]) * rdy;
+  const float Uw = n.unb_w + (DW - D0) * rdx - 0.5f * Gw * (A[0] + A[1]);
+  const float Ue = n.unb_e + (D0 - DE) * rdx - 0.5f * Ge * (A[2] + A[0]);
+  const float Vs = n.vnb_s + (DS - D0) * rdy - 0.5f * Gs * (A[0] + A[3]);
+  const float Vn = n.vnb_n + (D0 - DN) * rdy - 0.5f * Gn * (A[4] + A[0]);
+  float Wb = 0.f, Wt = 0.f;
+  if (k.hb) {
+    const float Z = k.dzb + (s[0] - s[5]) * rdz;
+    Wb = n.wnb_b + (DB - D0) * rdz - 0.5f * Z * k.rfb * (A[0] / k.rho + A[5] / k.rhom);
+  }
+  if (k.ht) {
+    const float Z = k.dzt + (s[6] - s[0]) * rdz;
+    Wt = n.wnb_t + (D0 - DT) * rdz - 0.5f * Z * k.rft * (A[6] / k.rhop + A[0] / k.rho);
+  }
+  AcOut o;
+  o.ub = Uw;
+  o.vb = Vs;
+  o.wb = Wb;
+  // pressure-gradient terms of the input pi' and theta_rho
+  const float c0 = -kHalfCp * dtau;
+  const float* p = n.p;
+  const float* t = n.t;
+  float pb = pnb0, tb = 0.f;
+  pb += Uw * c0 * (t[0] + t[1]) * rdx - Ue * c0 * (t[2] + t[0]) * rdx;
+  tb += Uw * c0 * (p[0] - p[1]) * rdx + Ue * c0 * (p[2] - p[0]) * rdx;
+  pb += Vs * c0 * (t[0] + t[3]) * rdy - Vn * c0 * (t[4] + t[0]) * rdy;
+  tb += Vs * c0 * (p[0] - p[3]) * rdy + Vn * c0 * (p[4] - p[0]) * rdy;
+  if (k.hb) {
+    pb += Wb * c0 * (t[0] + t[5]) * rdz;
+    tb += Wb * c0 * (p[0] - p[5]) * rdz;
+  }
+  if (k.ht) {
+    pb -= Wt * c0 * (t[6] + t[0]) * rdz;
+    tb += Wt * c0 * (p[6] - p[0]) * rdz;
+  }
+  o.pb = pb;
+  o.tb = tb;
+  // pi'_s: the divergence factor and advection_pi of this cell and its six neighbours
+  const float uw = n.un_w, ue = n.un_e, vs = n.vn_s, vn = n.vn_n;
+  const float wbn = k.hb ? n.wn_b : 0.f, wtn = k.ht ? n.wn_t : 0.f;
+  const float div = (ue - uw) * rdx + (vn - vs) * rdy + (wtn - wbn) * rdz;
+  const float dap = -(0.5f * (-ue * rdx + uw * rdx) + 0.5f * (-vn * rdy + vs * rdy) +
+                      ((k.hb ? 0.5f * k.rfb * wbn * rdz : 0.f) - (k.ht ? 0.5f * k.rft * wtn * rdz : 0.f)) / k.rho);
+  float sb = A[0] * (-kRdCvA * div + dap);
+  sb += A[2] * 0.5f * ue * rdx - A[1] * 0.5f * uw * rdx;
+  sb += A[4] * 0.5f * vn * rdy - A[3] * 0.5f * vs * rdy;
+  if (k.ht) sb += A[6] * 0.5f * k.rft * wtn * rdz / k.rhop;
+  if (k.hb) sb -= A[5] * 0.5f * k.rfb * wbn * rdz / k.rhom;
+  o.sb = sb;
+  return o;
+}
+
+__device__ __forceinline__ AcCol acoustic_col(const Cols& c, int k, int nz) {
+  AcCol q;
+  q.hb = k > 0;
+  q.ht = k + 1 < nz;
+  q.pi0 = c.pi0[k];
+  q.rho = c.rho[k];
+  q.pi0m = q.hb ? c.pi0[k - 1] : 0.f;
+  q.rhom = q.hb ? c.rho[k - 1] : 1.f;
+  q.pi0p = q.ht ? c.pi0[k + 1] : 0.f;
+  q.rhop = q.ht ? c.rho[k + 1] : 1.f;
+  q.rfb = c.rho_face[k];
+  q.rft = c.rho_face[k + 1];
+  q.dzb = c.dpi0dz[k];
+  q.dzt = c.dpi0dz[k + 1];
+  return q;
+}
+
+// one thread per cell (any nx)
 __global__ void __launch_bounds__(AB) k_acoustic_vjp(Dims d, Phys ph, Cols c, AcousticVjpArgs a, float dtau) {
   const long long t = (long long)blockIdx.x * AB + threadIdx.x;
   const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
   if (t >= d.cells()) return;
   const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
-  const int im = wrapx(i - 1, nx), ip = wrapx(i + 1, nx), jm = wrapx(j - 1, ny), jp = wrapx(j + 1, ny);
   const int id = (int)t, row = k * plane + j * nx;
-  const int cW = row + im, cE = row + ip, cS = k * plane + jm * nx + i, cN = k * plane + jp * nx + i;
-  const int cB = id - plane, cT = id + plane;
-  const bool hb = k > 0, ht = k + 1 < nz;
-  const float rdx = ph.rdx, rdy = ph.rdy, rdz = ph.rdz;
+  const AcCol col = acoustic_col(c, k, nz);
+  int q[7];
+  q[0] = id;
+  q[1] = row + wrapx(i - 1, nx);
+  q[2] = row + wrapx(i + 1, nx);
+  q[3] = k * plane + wrapx(j - 1, ny) * nx + i;
+  q[4] = k * plane + wrapx(j + 1, ny) * nx + i;
+  q[5] = col.hb ? id - plane : id;
+  q[6] = col.ht ? id + plane : id;
   const float K = kDivDamp * dtau;
-  auto Aof = [&](int q) { return K * LD(a.pnb, q); };
-  auto divb = [&](int q, int kk, float A) { return -A * kRdCvA * (c.pi0[kk] + LD(a.ps, q)); };
-  const float A0 = Aof(id), AW = Aof(cW), AE = Aof(cE), AS = Aof(cS), AN = Aof(cN);
-  const float AB_ = hb ? Aof(cB) : 0.f, AT = ht ? Aof(cT) : 0.f;
-  const float s0 = LD(a.ps, id), sW = LD(a.ps, cW), sE = LD(a.ps, cE), sS = LD(a.ps, cS), sN = LD(a.ps, cN);
-  const float sB = hb ? LD(a.ps, cB) : 0.f, sT = ht ? LD(a.ps, cT) : 0.f;
-  const float D0 = divb(id, k, A0), DW = divb(cW, k, AW), DE = divb(cE, k, AE), DS = divb(cS, k, AS),
-              DN = divb(cN, k, AN);
-  const float DB = hb ? divb(cB, k - 1, AB_) : 0.f, DT = ht ? divb(cT, k + 1, AT) : 0.f;
-  // adjoints of the new winds on the six faces of the cell
-  const float Gw = (s0 - sW) * rdx, Ge = (sE - s0) * rdx, Gs = (s0 - sS) * rdy, Gn = (sN - s0) * rdy;
-  const float Uw = LD(a.unb, id) + (DW - D0) * rdx - 0.5f * Gw * (A0 + AW);
-  const float Ue = LD(a.unb, cE) + (D0 - DE) * rdx - 0.5f * Ge * (AE + A0);
-  const float Vs = LD(a.vnb, id) + (DS - D0) * rdy - 0.5f * Gs * (A0 + AS);
-  const float Vn = LD(a.vnb, cN) + (D0 - DN) * rdy - 0.5f * Gn * (AN + A0);
-  const float rho = c.rho[k];
-  float Wb = 0.f, Wt = 0.f;
-  if (hb) {
-    const float Z = c.dpi0dz[k] + (s0 - sB) * rdz;
-    Wb = LD(a.wnb, id) + (DB - D0) * rdz - 0.5f * Z * c.rho_face[k] * (A0 / rho + AB_ / c.rho[k - 1]);
+  AcNbr n;
+#pragma unroll
+  for (int m = 0; m < 7; ++m) {
+    const bool ok = (m < 5) || (m == 5 ? col.hb : col.ht);
+    n.A[m] = ok ? K * LD(a.pnb, q[m]) : 0.f;
+    n.s[m] = ok ? LD(a.ps, q[m]) : 0.f;
+    n.p[m] = ok ? LD(a.p, q[m]) : 0.f;
+    n.t[m] = ok ? LD(a.trho, q[m]) : 0.f;
   }
-  if (ht) {
-    const float Z = c.dpi0dz[k + 1] + (sT - s0) * rdz;
-    Wt = LD(a.wnb, cT) + (D0 - DT) * rdz - 0.5f * Z * c.rho_face[k + 1] * (AT / c.rho[k + 1] + A0 / rho);
-  }
-  // old winds: identity; slow tendencies: dtau
-  a.ub[id] = Uw;
-  a.vb[id] = Vs;
-  a.wb[id] = Wb;
+  n.unb_w = LD(a.unb, id); n.unb_e = LD(a.unb, q[2]);
+  n.vnb_s = LD(a.vnb, id); n.vnb_n = LD(a.vnb, q[4]);
+  n.wnb_b = LD(a.wnb, id); n.wnb_t = LD(a.wnb, id + plane);
+  n.un_w = LD(a.un, id); n.un_e = LD(a.un, q[2]);
+  n.vn_s = LD(a.vn, id); n.vn_n = LD(a.vn, q[4]);
+  n.wn_b = LD(a.wn, id); n.wn_t = LD(a.wn, id + plane);
+  const AcOut o = acoustic_vjp_cell(n, col, LD(a.pnb, id), ph.rdx, ph.rdy, ph.rdz, dtau);
+  a.ub[id] = o.ub;
+  a.vb[id] = o.vb;
+  a.wb[id] = o.wb;
   if (k == nz - 1) a.wb[id + plane] = 0.f;
-  a.Rub[id] += Uw * dtau;
-  a.Rvb[id] += Vs * dtau;
-  if (hb) a.Rwb[id] += Wb * dtau;
-  // pressure-gradient terms: pi' and theta_rho of the old state
-  const float p0 = LD(a.p, id), t0 = LD(a.trho, id);
-  const float c0 = -kHalfCp * dtau;
-  float pb = LD(a.pnb, id), tb = 0.f;
-  {
-    const float pw = LD(a.p, cW), tw = LD(a.trho, cW), pe = LD(a.p, cE), te = LD(a.trho, cE);
-    pb += Uw * c0 * (t0 + tw) * rdx - Ue * c0 * (te + t0) * rdx;
-    tb += Uw * c0 * (p0 - pw) * rdx + Ue * c0 * (pe - p0) * rdx;
-    const float ps_ = LD(a.p, cS), ts = LD(a.trho, cS), pn = LD(a.p, cN), tn = LD(a.trho, cN);
-    pb += Vs * c0 * (t0 + ts) * rdy - Vn * c0 * (tn + t0) * rdy;
-    tb += Vs * c0 * (p0 - ps_) * rdy + Vn * c0 * (pn - p0) * rdy;
-    if (hb) {
-      const float pbm = LD(a.p, cB), tbm = LD(a.trho, cB);
-      pb += Wb * c0 * (t0 + tbm) * rdz;
-      tb += Wb * c0 * (p0 - pbm) * rdz;
-    }
-    if (ht) {
-      const float ptp = LD(a.p, cT), ttp = LD(a.trho, cT);
-      pb -= Wt * c0 * (ttp + t0) * rdz;
-      tb += Wt * c0 * (ptp - p0) * rdz;
-    }
-  }
-  a.pb[id] = pb;
-  a.trhob[id] += tb;
-  // pi'_s: the divergence factor and advection_pi of this cell and its six neighbours
-  const float uw = LD(a.un, id), ue = LD(a.un, cE), vs = LD(a.vn, id), vn = LD(a.vn, cN);
-  const float wbn = hb ? LD(a.wn, id) : 0.f, wtn = ht ? LD(a.wn, cT) : 0.f;
-  const float div = (ue - uw) * rdx + (vn - vs) * rdy + (wtn - wbn) * rdz;
-  const float dap = -(0.5f * (-ue * rdx + uw * rdx) + 0.5f * (-vn * rdy + vs * rdy) +
-                      ((hb ? 0.5f * c.rho_face[k] * wbn * rdz : 0.f) - (ht ? 0.5f * c.rho_face[k + 1] * wtn * rdz : 0.f)) /
-                          rho);
-  float sb = A0 * (-kRdCvA * div + dap);
-  sb += AE * 0.5f * ue * rdx - AW * 0.5f * uw * rdx;
-  sb += AN * 0.5f * vn * rdy - AS * 0.5f * vs * rdy;
-  if (ht) sb += AT * 0.5f * c.rho_face[k + 1] * wtn * rdz / c.rho[k + 1];
-  if (hb) sb -= AB_ * 0.5f * c.rho_face[k] * wbn * rdz / c.rho[k - 1];
-  a.psb[id] += sb;
+  a.pb[id] = o.pb;
+  a.Rub[id] += o.ub * dtau;
+  a.Rvb[id] += o.vb * dtau;
+  if (col.hb) a.Rwb[id] += o.wb * dtau;
+  a.trhob[id] += o.tb;
+  a.psb[id] += o.sb;
 }
 
+// four consecutive x cells per thread with float4 rows (nx % 4 == 0), as k_acoustic_vec
+__device__ __forceinline__ float4 ld4(const float* p, int i) { return __ldg(reinterpret_cast<const float4*>(p + i)); }
+__device__ __forceinline__ float f4(const float4& v, int l) { return l == 0 ? v.x : (l == 1 ? v.y : (l == 2 ? v.z : v.w)); }
+
+__global__ void __launch_bounds__(64) k_acoustic_vjp4(Dims d, Phys ph, Cols c, AcousticVjpArgs a, float dtau) {
+  const int nq = d.nx / 4;
+  const int qx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (qx >= nq || j >= d.ny) return;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
+  const int i0 = 4 * qx;
+  const int r0 = k * plane + j * nx, rs = k * plane + wrapx(j - 1, ny) * nx, rn = k * plane + wrapx(j + 1, ny) * nx;
+  const int iw = wrapx(i0 - 1, nx), ie = wrapx(i0 + 4, nx);
+  const AcCol col = acoustic_col(c, k, nz);
+  const int rb = col.hb ? r0 - plane : r0, rt = col.ht ? r0 + plane : r0;
+  const float K = kDivDamp * dtau;
+  // rows: 0 centre, 1 south, 2 north, 3 below, 4 above
+  const int rows[5] = {r0, rs, rn, rb, rt};
+  float4 PN[5], PS[5], PP[5], TT[5];
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    PN[r] = ld4(a.pnb, rows[r] + i0);
+    PS[r] = ld4(a.ps, rows[r] + i0);
+    PP[r] = ld4(a.p, rows[r] + i0);
+    TT[r] = ld4(a.trho, rows[r] + i0);
+  }
+  const float pnW = LD(a.pnb, r0 + iw), pnE = LD(a.pnb, r0 + ie);
+  const float psW = LD(a.ps, r0 + iw), psE = LD(a.ps, r0 + ie);
+  const float ppW = LD(a.p, r0 + iw), ppE = LD(a.p, r0 + ie);
+  const float ttW = LD(a.trho, r0 + iw), ttE = LD(a.trho, r0 + ie);
+  const float4 UNB = ld4(a.unb, r0 + i0), VNB = ld4(a.vnb, r0 + i0), VNBn = ld4(a.vnb, rn + i0);
+  const float4 WNB = ld4(a.wnb, r0 + i0), WNBt = ld4(a.wnb, r0 + plane + i0);
+  const float4 UN = ld4(a.un, r0 + i0), VN = ld4(a.vn, r0 + i0), VNn = ld4(a.vn, rn + i0);
+  const float4 WN = ld4(a.wn, r0 + i0), WNt = ld4(a.wn, r0 + plane + i0);
+  const float unbE = LD(a.unb, r0 + ie), unE = LD(a.un, r0 + ie);
+  float ob[4], vb[4], wb[4], pb[4], tb[4], sb[4];
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    AcNbr n;
+    // x neighbours inside the vector or the scalar ends
+    const float pnw = l == 0 ? pnW : f4(PN[0], l - 1), pne = l == 3 ? pnE : f4(PN[0], l + 1);
+    const float psw = l == 0 ? psW : f4(PS[0], l - 1), pse = l == 3 ? psE : f4(PS[0], l + 1);
+    const float ppw = l == 0 ? ppW : f4(PP[0], l - 1), ppe = l == 3 ? ppE : f4(PP[0], l + 1);
+    const float ttw = l == 0 ? ttW : f4(TT[0], l - 1), tte = l == 3 ? ttE : f4(TT[0], l + 1);
+    n.A[0] = K * f4(PN[0], l); n.A[1] = K * pnw; n.A[2] = K * pne;
+    n.A[3] = K * f4(PN[1], l); n.A[4] = K * f4(PN[2], l);
+    n.A[5] = col.hb ? K * f4(PN[3], l) : 0.f; n.A[6] = col.ht ? K * f4(PN[4], l) : 0.f;
+    n.s[0] = f4(PS[0], l); n.s[1] = psw; n.s[2] = pse; n.s[3] = f4(PS[1], l); n.s[4] = f4(PS[2], l);
+    n.s[5] = f4(PS[3], l); n.s[6] = f4(PS[4], l);
+    n.p[0] = f4(PP[0], l); n.p[1] = ppw; n.p[2] = ppe; n.p[3] = f4(PP[1], l); n.p[4] = f4(PP[2], l);
+    n.p[5] = f4(PP[3], l); n.p[6] = f4(PP[4], l);
+    n.t[0] = f4(TT[0], l); n.t[1] = ttw; n.t[2] = tte; n.t[3] = f4(TT[1], l); n.t[4] = f4(TT[2], l);
+    n.t[5] = f4(TT[3], l); n.t[6] = f4(TT[4], l);
+    n.unb_w = f4(UNB, l); n.unb_e = l == 3 ? unbE : f4(UNB, l + 1);
+    n.vnb_s = f4(VNB, l); n.vnb_n = f4(VNBn, l);
+    n.wnb_b = f4(WNB, l); n.wnb_t = f4(WNBt, l);
+    n.un_w = f4(UN, l); n.un_e = l == 3 ? unE : f4(UN, l + 1);
+    n.vn_s = f4(VN, l); n.vn_n = f4(VNn, l);
+    n.wn_b = f4(WN, l); n.wn_t = f4(WNt, l);
+    const AcOut o = acoustic_vjp_cell(n, col, f4(PN[0], l), ph.rdx, ph.rdy, ph.rdz, dtau);
+    ob[l] = o.ub; vb[l] = o.vb; wb[l] = o.wb; pb[l] = o.pb; tb[l] = o.tb; sb[l] = o.sb;
+  }
+  auto st4 = [&](float* p, const float* v) { *reinterpret_cast<float4*>(p + r0 + i0) = make_float4(v[0], v[1], v[2], v[3]); };
+  auto acc4 = [&](float* p, const float* v, float f) {
+    float4* q = reinterpret_cast<float4*>(p + r0 + i0);
+    float4 x = *q;
+    x.x += v[0] * f; x.y += v[1] * f; x.z += v[2] * f; x.w += v[3] * f;
+    *q = x;
+  };
+  st4(a.ub, ob);
+  st4(a.vb, vb);
+  st4(a.wb, wb);
+  st4(a.pb, pb);
+  if (k == nz - 1) *reinterpret_cast<float4*>(a.wb + r0 + plane + i0) = make_float4(0.f, 0.f, 0.f, 0.f);
+  acc4(a.Rub, ob, dtau);
+  acc4(a.Rvb, vb, dtau);
+  if (col.hb) acc4(a.Rwb, wb, dtau);
+  acc4(a.trhob, tb, 1.f);
+  acc4(a.psb, sb, 1.f);
+}
 // ---------------------------------------------------------------------------------------------
 // pointwise part of a stage's reverse pass (after the acoustic loop):
 //   cbar of the five advected fields, the phi*div terms, Coriolis, buoyancy, theta_rho,
@@ -518,9 +654,9 @@ __global__ void __launch_bounds__(AB) k_smag_lin(Dims d, Phys ph, Cols c, State 
   const float s12 = r * (0.25f * (e12(d, ph, s, i, j, k) + e12(d, ph, s, i + 1, j + 1, k) + e12(d, ph, s, i, j + 1, k) +
                                   e12(d, ph, s, i + 1, j, k)));
   float s13 = 0.f, s23 = 0.f, n2 = 0.f;
-  int ks[4];
-  (void)ks;
-  for (int f = 1; f < nz; ++f) {  // sum over the faces with nonzero weight
+  // faces with nonzero weight: k, k+1 inside, 1..3 / nz-3..nz-1 in the end cells
+  const int f0 = k == 0 ? 1 : (k == nz - 1 ? nz - 3 : k), f1 = k == 0 ? 3 : (k == nz - 1 ? nz - 1 : k + 1);
+  for (int f = f0; f <= f1; ++f) {
     const float we = w_edge(k, f, nz), wn = w_n2(k, f, nz);
     if (we != 0.f) {
       s13 += we * (e13(d, ph, s, i, j, f) + e13(d, ph, s, i + 1, j, f));
@@ -741,6 +877,14 @@ __global__ void __launch_bounds__(AB) k_smag_state_vjp(Dims d, Phys ph, Cols c, 
 
 cudaError_t launch_acoustic_vjp(const Dims& d, const Phys& ph, const Cols& c, const AcousticVjpArgs& a, float dtau,
                                 cudaStream_t st) {
+  if (d.nx % 4 == 0) {
+    // small blocks: the kernel holds 164 registers per thread (a register cap that made it spill
+    // float4 values faulted with a misaligned address)
+    dim3 b(16, 4, 1);
+    dim3 g((d.nx / 4 + 15) / 16, (d.ny + 3) / 4, d.nz);
+    k_acoustic_vjp4<<<g, b, 0, st>>>(d, ph, c, a, dtau);
+    return cudaGetLastError();
+  }
   const unsigned g = (unsigned)((d.cells() + AB - 1) / AB);
   k_acoustic_vjp<<<g, AB, 0, st>>>(d, ph, c, a, dtau);
   return cudaGetLastError();

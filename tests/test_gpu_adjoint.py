@@ -106,3 +106,29 @@ def test_reverse_mode_matches_oracle_finite_differences(built_lib, nstages, only
     S.close()
     REPORT["%d_%s_%d" % (nstages, only, turb)] = errs
     assert all(e[2] <= TOL for e in errs), errs
+
+
+def test_kept_step_reverse_equals_recomputed_reverse(built_lib):
+    """lexgb_step_keep + lexgb_step_vjp_kept (intermediates from the forward) gives the same adjoint
+    as lexgb_step_vjp (recomputed), and the kept forward advances the state like lexgb_step."""
+    import ctypes
+    from lex_gb300 import _lib
+    g, D, S, x0, forward = _setup(3, 1)
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    rng = np.random.default_rng(11)
+    yb = _direction(rng, nx, ny, nz)
+    ref = S.step_vjp(yb, nstages=3)
+    S.step(1)
+    stepped = S.download()
+    S.upload(x0)
+    _lib.check(S.lib.lexgb_step_keep(S.handle))
+    kept_state = S.download()
+    dev = [np.ascontiguousarray(np.asarray(a, np.float32).transpose(2, 1, 0)) for a in yb]
+    out = [np.empty_like(a) for a in dev]
+    _lib.check(S.lib.lexgb_step_vjp_kept(S.handle, (ctypes.c_void_p * 6)(*[a.ctypes.data for a in dev]),
+                                         (ctypes.c_void_p * 6)(*[a.ctypes.data for a in out]), 0))
+    S.close()
+    for a, b in zip(kept_state, stepped):
+        np.testing.assert_array_equal(a, b)
+    for a, b in zip(out, ref):
+        np.testing.assert_array_equal(a.transpose(2, 1, 0), b)
