@@ -176,7 +176,7 @@ int run_stage(lexgb_ctx* c, int s, const State& xi0, const State& xis, const Sta
   for (int l = 1; l <= launches; ++l) {
     AcousticOut tgt = (l == launches && !(alias && launches == 1)) ? O : ((l & 1) ? X : Y);
     if (l <= nsingle)
-      CK(launch_acoustic(c->d, c->ph, c->cols, in, tgt, dtau, c->stream));
+      CK(launch_acoustic(c->d, c->ph, c->cols, in, tgt, dtau, c->stream, l & 1));
     else
       CK(launch_acoustic_pair(c->d, c->ph, c->cols, in, tgt, dtau, c->stream));
     in.u = tgt.u;
@@ -687,7 +687,7 @@ int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
     switch (which) {
       case LEXGB_KERNEL_ACOUSTIC: {
         const AcousticOut o = (r & 1) ? Y : X;
-        cudaError_t e = launch_acoustic(d, c->ph, c->cols, in, o, (float)p.dtau[2], c->stream);
+        cudaError_t e = launch_acoustic(d, c->ph, c->cols, in, o, (float)p.dtau[2], c->stream, r & 1);
         in.u = o.u; in.v = o.v; in.w = o.w; in.p = o.p;
         return e;
       }

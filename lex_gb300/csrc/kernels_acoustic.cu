@@ -142,11 +142,15 @@ __device__ __forceinline__ void zero(float (&o)[V]) {
 
 template <int V>
 __global__ void __launch_bounds__(256) k_acoustic_vec(Dims d, Phys ph, Cols c, AcousticIn a, AcousticOut o,
-                                                      float dtau) {
+                                                      float dtau, int rev) {
   const int nq = d.nx / V;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
+  // rev: blocks walk the grid in reverse order, so that a sub-step following one in forward order
+  // starts on the fields its predecessor wrote last (still in L2)
+  const int bx = rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+  const int by = rev ? gridDim.y - 1 - blockIdx.y : blockIdx.y;
+  const int q = bx * blockDim.x + threadIdx.x;
+  const int j = by * blockDim.y + threadIdx.y;
+  const int k = rev ? gridDim.z - 1 - blockIdx.z : blockIdx.z;
   if (q >= nq || j >= d.ny) return;
   const int nx = d.nx, nz = d.nz;
   const int i0 = q * V;
@@ -742,7 +746,7 @@ __global__ void k_diag_advpi(Dims d, Phys ph, Cols c, const float* __restrict__ 
 }  // namespace
 
 cudaError_t launch_acoustic(const Dims& d, const Phys& ph, const Cols& c, AcousticIn in, AcousticOut out, float dtau,
-                            cudaStream_t st) {
+                            cudaStream_t st, int rev) {
   constexpr int VW = ACOUSTIC_VEC;
 #if ACOUSTIC_ZMARCH > 0
   if (d.nx % VW == 0) {
@@ -757,7 +761,7 @@ cudaError_t launch_acoustic(const Dims& d, const Phys& ph, const Cols& c, Acoust
     const int nq = d.nx / VW;
     dim3 b(VW == 4 ? 16 : 32, VW == 4 ? 16 : 8, 1);
     dim3 g((nq + b.x - 1) / b.x, (d.ny + b.y - 1) / b.y, d.nz);
-    k_acoustic_vec<VW><<<g, b, 0, st>>>(d, ph, c, in, out, dtau);
+    k_acoustic_vec<VW><<<g, b, 0, st>>>(d, ph, c, in, out, dtau, rev);
     return cudaGetLastError();
   }
   dim3 g((d.nx + BX - 1) / BX, (d.ny + BY - 1) / BY, (d.nz + BZ - 1) / BZ);

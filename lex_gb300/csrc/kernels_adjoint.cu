@@ -293,87 +293,132 @@ __global__ void __launch_bounds__(AB) k_acoustic_vjp(Dims d, Phys ph, Cols c, Ac
   a.psb[id] += o.sb;
 }
 
-// four consecutive x cells per thread with float4 rows (nx % 4 == 0), as k_acoustic_vec
-__device__ __forceinline__ float4 ld4(const float* p, int i) { return __ldg(reinterpret_cast<const float4*>(p + i)); }
-__device__ __forceinline__ float f4(const float4& v, int l) { return l == 0 ? v.x : (l == 1 ? v.y : (l == 2 ? v.z : v.w)); }
+// V consecutive x cells per thread (V = 2 or 4) with V-wide row loads (nx % V == 0), as
+// k_acoustic_vec
+#ifndef ACOUSTIC_VJP_VEC
+#define ACOUSTIC_VJP_VEC 4
+#endif
+template <int V>
+struct VecF;
+template <>
+struct VecF<4> {
+  typedef float4 T;
+};
+template <>
+struct VecF<2> {
+  typedef float2 T;
+};
+template <int V>
+__device__ __forceinline__ void ldvec(const float* p, int i, float (&o)[V]) {
+  typedef typename VecF<V>::T T;
+  const T t = __ldg(reinterpret_cast<const T*>(p + i));
+  const float* f = reinterpret_cast<const float*>(&t);
+#pragma unroll
+  for (int l = 0; l < V; ++l) o[l] = f[l];
+}
+template <int V>
+__device__ __forceinline__ void stvec(float* p, int i, const float (&v)[V]) {
+  typedef typename VecF<V>::T T;
+  T t;
+  float* f = reinterpret_cast<float*>(&t);
+#pragma unroll
+  for (int l = 0; l < V; ++l) f[l] = v[l];
+  *reinterpret_cast<T*>(p + i) = t;
+}
+template <int V>
+__device__ __forceinline__ void accvec(float* p, int i, const float (&v)[V], float s) {
+  typedef typename VecF<V>::T T;
+  T t = *reinterpret_cast<T*>(p + i);
+  float* f = reinterpret_cast<float*>(&t);
+#pragma unroll
+  for (int l = 0; l < V; ++l) f[l] += v[l] * s;
+  *reinterpret_cast<T*>(p + i) = t;
+}
 
-__global__ void __launch_bounds__(64) k_acoustic_vjp4(Dims d, Phys ph, Cols c, AcousticVjpArgs a, float dtau) {
-  const int nq = d.nx / 4;
+template <int V>
+__global__ void __launch_bounds__(64) k_acoustic_vjpv(Dims d, Phys ph, Cols c, AcousticVjpArgs a, float dtau) {
+  const int nq = d.nx / V;
   const int qx = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   if (qx >= nq || j >= d.ny) return;
   const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
-  const int i0 = 4 * qx;
+  const int i0 = V * qx;
   const int r0 = k * plane + j * nx, rs = k * plane + wrapx(j - 1, ny) * nx, rn = k * plane + wrapx(j + 1, ny) * nx;
-  const int iw = wrapx(i0 - 1, nx), ie = wrapx(i0 + 4, nx);
+  const int iw = wrapx(i0 - 1, nx), ie = wrapx(i0 + V, nx);
   const AcCol col = acoustic_col(c, k, nz);
   const int rb = col.hb ? r0 - plane : r0, rt = col.ht ? r0 + plane : r0;
   const float K = kDivDamp * dtau;
   // rows: 0 centre, 1 south, 2 north, 3 below, 4 above
   const int rows[5] = {r0, rs, rn, rb, rt};
-  float4 PN[5], PS[5], PP[5], TT[5];
+  float PN[5][V], PS[5][V], PP[5][V], TT[5][V];
 #pragma unroll
   for (int r = 0; r < 5; ++r) {
-    PN[r] = ld4(a.pnb, rows[r] + i0);
-    PS[r] = ld4(a.ps, rows[r] + i0);
-    PP[r] = ld4(a.p, rows[r] + i0);
-    TT[r] = ld4(a.trho, rows[r] + i0);
+    ldvec<V>(a.pnb, rows[r] + i0, PN[r]);
+    ldvec<V>(a.ps, rows[r] + i0, PS[r]);
+    ldvec<V>(a.p, rows[r] + i0, PP[r]);
+    ldvec<V>(a.trho, rows[r] + i0, TT[r]);
   }
   const float pnW = LD(a.pnb, r0 + iw), pnE = LD(a.pnb, r0 + ie);
   const float psW = LD(a.ps, r0 + iw), psE = LD(a.ps, r0 + ie);
   const float ppW = LD(a.p, r0 + iw), ppE = LD(a.p, r0 + ie);
   const float ttW = LD(a.trho, r0 + iw), ttE = LD(a.trho, r0 + ie);
-  const float4 UNB = ld4(a.unb, r0 + i0), VNB = ld4(a.vnb, r0 + i0), VNBn = ld4(a.vnb, rn + i0);
-  const float4 WNB = ld4(a.wnb, r0 + i0), WNBt = ld4(a.wnb, r0 + plane + i0);
-  const float4 UN = ld4(a.un, r0 + i0), VN = ld4(a.vn, r0 + i0), VNn = ld4(a.vn, rn + i0);
-  const float4 WN = ld4(a.wn, r0 + i0), WNt = ld4(a.wn, r0 + plane + i0);
+  float UNB[V], VNB[V], VNBn[V], WNB[V], WNBt[V], UN[V], VN[V], VNn[V], WN[V], WNt[V];
+  ldvec<V>(a.unb, r0 + i0, UNB);
+  ldvec<V>(a.vnb, r0 + i0, VNB);
+  ldvec<V>(a.vnb, rn + i0, VNBn);
+  ldvec<V>(a.wnb, r0 + i0, WNB);
+  ldvec<V>(a.wnb, r0 + plane + i0, WNBt);
+  ldvec<V>(a.un, r0 + i0, UN);
+  ldvec<V>(a.vn, r0 + i0, VN);
+  ldvec<V>(a.vn, rn + i0, VNn);
+  ldvec<V>(a.wn, r0 + i0, WN);
+  ldvec<V>(a.wn, r0 + plane + i0, WNt);
   const float unbE = LD(a.unb, r0 + ie), unE = LD(a.un, r0 + ie);
-  float ob[4], vb[4], wb[4], pb[4], tb[4], sb[4];
+  float ob[V], vb[V], wb[V], pb[V], tb[V], sb[V];
 #pragma unroll
-  for (int l = 0; l < 4; ++l) {
+  for (int l = 0; l < V; ++l) {
     AcNbr n;
     // x neighbours inside the vector or the scalar ends
-    const float pnw = l == 0 ? pnW : f4(PN[0], l - 1), pne = l == 3 ? pnE : f4(PN[0], l + 1);
-    const float psw = l == 0 ? psW : f4(PS[0], l - 1), pse = l == 3 ? psE : f4(PS[0], l + 1);
-    const float ppw = l == 0 ? ppW : f4(PP[0], l - 1), ppe = l == 3 ? ppE : f4(PP[0], l + 1);
-    const float ttw = l == 0 ? ttW : f4(TT[0], l - 1), tte = l == 3 ? ttE : f4(TT[0], l + 1);
-    n.A[0] = K * f4(PN[0], l); n.A[1] = K * pnw; n.A[2] = K * pne;
-    n.A[3] = K * f4(PN[1], l); n.A[4] = K * f4(PN[2], l);
-    n.A[5] = col.hb ? K * f4(PN[3], l) : 0.f; n.A[6] = col.ht ? K * f4(PN[4], l) : 0.f;
-    n.s[0] = f4(PS[0], l); n.s[1] = psw; n.s[2] = pse; n.s[3] = f4(PS[1], l); n.s[4] = f4(PS[2], l);
-    n.s[5] = f4(PS[3], l); n.s[6] = f4(PS[4], l);
-    n.p[0] = f4(PP[0], l); n.p[1] = ppw; n.p[2] = ppe; n.p[3] = f4(PP[1], l); n.p[4] = f4(PP[2], l);
-    n.p[5] = f4(PP[3], l); n.p[6] = f4(PP[4], l);
-    n.t[0] = f4(TT[0], l); n.t[1] = ttw; n.t[2] = tte; n.t[3] = f4(TT[1], l); n.t[4] = f4(TT[2], l);
-    n.t[5] = f4(TT[3], l); n.t[6] = f4(TT[4], l);
-    n.unb_w = f4(UNB, l); n.unb_e = l == 3 ? unbE : f4(UNB, l + 1);
-    n.vnb_s = f4(VNB, l); n.vnb_n = f4(VNBn, l);
-    n.wnb_b = f4(WNB, l); n.wnb_t = f4(WNBt, l);
-    n.un_w = f4(UN, l); n.un_e = l == 3 ? unE : f4(UN, l + 1);
-    n.vn_s = f4(VN, l); n.vn_n = f4(VNn, l);
-    n.wn_b = f4(WN, l); n.wn_t = f4(WNt, l);
-    const AcOut o = acoustic_vjp_cell(n, col, f4(PN[0], l), ph.rdx, ph.rdy, ph.rdz, dtau);
+    const float pnw = l == 0 ? pnW : PN[0][l - 1], pne = l == V - 1 ? pnE : PN[0][l + 1];
+    const float psw = l == 0 ? psW : PS[0][l - 1], pse = l == V - 1 ? psE : PS[0][l + 1];
+    const float ppw = l == 0 ? ppW : PP[0][l - 1], ppe = l == V - 1 ? ppE : PP[0][l + 1];
+    const float ttw = l == 0 ? ttW : TT[0][l - 1], tte = l == V - 1 ? ttE : TT[0][l + 1];
+    n.A[0] = K * PN[0][l]; n.A[1] = K * pnw; n.A[2] = K * pne;
+    n.A[3] = K * PN[1][l]; n.A[4] = K * PN[2][l];
+    n.A[5] = col.hb ? K * PN[3][l] : 0.f; n.A[6] = col.ht ? K * PN[4][l] : 0.f;
+    n.s[0] = PS[0][l]; n.s[1] = psw; n.s[2] = pse; n.s[3] = PS[1][l]; n.s[4] = PS[2][l];
+    n.s[5] = PS[3][l]; n.s[6] = PS[4][l];
+    n.p[0] = PP[0][l]; n.p[1] = ppw; n.p[2] = ppe; n.p[3] = PP[1][l]; n.p[4] = PP[2][l];
+    n.p[5] = PP[3][l]; n.p[6] = PP[4][l];
+    n.t[0] = TT[0][l]; n.t[1] = ttw; n.t[2] = tte; n.t[3] = TT[1][l]; n.t[4] = TT[2][l];
+    n.t[5] = TT[3][l]; n.t[6] = TT[4][l];
+    n.unb_w = UNB[l]; n.unb_e = l == V - 1 ? unbE : UNB[l + 1];
+    n.vnb_s = VNB[l]; n.vnb_n = VNBn[l];
+    n.wnb_b = WNB[l]; n.wnb_t = WNBt[l];
+    n.un_w = UN[l]; n.un_e = l == V - 1 ? unE : UN[l + 1];
+    n.vn_s = VN[l]; n.vn_n = VNn[l];
+    n.wn_b = WN[l]; n.wn_t = WNt[l];
+    const AcOut o = acoustic_vjp_cell(n, col, PN[0][l], ph.rdx, ph.rdy, ph.rdz, dtau);
     ob[l] = o.ub; vb[l] = o.vb; wb[l] = o.wb; pb[l] = o.pb; tb[l] = o.tb; sb[l] = o.sb;
   }
-  auto st4 = [&](float* p, const float* v) { *reinterpret_cast<float4*>(p + r0 + i0) = make_float4(v[0], v[1], v[2], v[3]); };
-  auto acc4 = [&](float* p, const float* v, float f) {
-    float4* q = reinterpret_cast<float4*>(p + r0 + i0);
-    float4 x = *q;
-    x.x += v[0] * f; x.y += v[1] * f; x.z += v[2] * f; x.w += v[3] * f;
-    *q = x;
-  };
-  st4(a.ub, ob);
-  st4(a.vb, vb);
-  st4(a.wb, wb);
-  st4(a.pb, pb);
-  if (k == nz - 1) *reinterpret_cast<float4*>(a.wb + r0 + plane + i0) = make_float4(0.f, 0.f, 0.f, 0.f);
-  acc4(a.Rub, ob, dtau);
-  acc4(a.Rvb, vb, dtau);
-  if (col.hb) acc4(a.Rwb, wb, dtau);
-  acc4(a.trhob, tb, 1.f);
-  acc4(a.psb, sb, 1.f);
+  stvec<V>(a.ub, r0 + i0, ob);
+  stvec<V>(a.vb, r0 + i0, vb);
+  stvec<V>(a.wb, r0 + i0, wb);
+  stvec<V>(a.pb, r0 + i0, pb);
+  if (k == nz - 1) {
+    float z[V];
+#pragma unroll
+    for (int l = 0; l < V; ++l) z[l] = 0.f;
+    stvec<V>(a.wb, r0 + plane + i0, z);
+  }
+  accvec<V>(a.Rub, r0 + i0, ob, dtau);
+  accvec<V>(a.Rvb, r0 + i0, vb, dtau);
+  if (col.hb) accvec<V>(a.Rwb, r0 + i0, wb, dtau);
+  accvec<V>(a.trhob, r0 + i0, tb, 1.f);
+  accvec<V>(a.psb, r0 + i0, sb, 1.f);
 }
+
 // ---------------------------------------------------------------------------------------------
 // pointwise part of a stage's reverse pass (after the acoustic loop):
 //   cbar of the five advected fields, the phi*div terms, Coriolis, buoyancy, theta_rho,
@@ -878,12 +923,13 @@ __global__ void __launch_bounds__(AB) k_smag_state_vjp(Dims d, Phys ph, Cols c, 
 
 cudaError_t launch_acoustic_vjp(const Dims& d, const Phys& ph, const Cols& c, const AcousticVjpArgs& a, float dtau,
                                 cudaStream_t st) {
-  if (d.nx % 4 == 0) {
-    // small blocks: the kernel holds 164 registers per thread (a register cap that made it spill
+  constexpr int V = ACOUSTIC_VJP_VEC;
+  if (d.nx % V == 0) {
+    // small blocks: many registers per thread (a register cap that made the 4-wide kernel spill
     // float4 values faulted with a misaligned address)
     dim3 b(16, 4, 1);
-    dim3 g((d.nx / 4 + 15) / 16, (d.ny + 3) / 4, d.nz);
-    k_acoustic_vjp4<<<g, b, 0, st>>>(d, ph, c, a, dtau);
+    dim3 g((d.nx / V + 15) / 16, (d.ny + 3) / 4, d.nz);
+    k_acoustic_vjpv<V><<<g, b, 0, st>>>(d, ph, c, a, dtau);
     return cudaGetLastError();
   }
   const unsigned g = (unsigned)((d.cells() + AB - 1) / AB);

@@ -284,7 +284,7 @@ struct AcousticIn {
 };
 struct AcousticOut { float *u, *v, *w, *p; };
 cudaError_t launch_acoustic(const Dims&, const Phys&, const Cols&, AcousticIn in, AcousticOut out, float dtau,
-                            cudaStream_t);
+                            cudaStream_t, int rev = 0);
 // two sub-steps in one launch (temporal blocking); in and out must not alias
 cudaError_t launch_acoustic_pair(const Dims&, const Phys&, const Cols&, AcousticIn in, AcousticOut out, float dtau,
                                  cudaStream_t);
