@@ -208,6 +208,29 @@ int lexgb_step_vjp(lexgb_ctx *ctx, int nstages, const float *const ybar[6], floa
 int lexgb_step_keep(lexgb_ctx *ctx);
 int lexgb_step_vjp_kept(lexgb_ctx *ctx, const float *const ybar[6], float *xbar[6], int on_device);
 
+/* ---- learned SGS correction: the 3-D CNN of dl_models.py:19-30 (simpleCNN) ----
+ * Device pointers, ordered on `stream` (a cudaStream_t; NULL: the default stream).  Activations
+ * are channels-innermost [nz][ny][nx][C]; BF16 where `void *`.
+ * lexgb_cnn_conv3d: one 3x3x3 zero-padded convolution on the BF16 tensor cores with FP32
+ *   accumulation: y = act(conv(x, w) + bias); nx a multiple of 16, cin a multiple of 16 (padding
+ *   channels of x zero), cout 8, 16 or 32; w [27][cout][cin] BF16 (offset (dz+1)*9+(dy+1)*3+(dx+1));
+ *   optional outputs: pre (FP32 pre-activation), y_bf16, y_f32; gelu: tanh-GELU (flax nn.gelu);
+ *   output channels >= creal are written as zero.  With the offsets mirrored and cin/cout swapped
+ *   in w it is the gradient with respect to the input.
+ * lexgb_cnn_gelu_bwd: g = dy * GELU'(pre) (pre NULL: g = dy), FP32 [npts][c] -> BF16 [npts][cpad].
+ * lexgb_cnn_conv3d_dw: dw[27][cout][cin] += sum_p g[p][co] x[p+off][ci], db[cout] += sum_p g[p][co]
+ *   (FP32, accumulated: zero them first); g has `gstride` channels per point.
+ * lexgb_cnn_adam: Adam step `step` (>= 1) of n FP32 parameters with moments m, v; optional BF16 copy.
+ * Replace flax's Conv / optax in lex_dl_train.py (the reference trains with optax.lamb). */
+int lexgb_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const void *x, const void *w, const float *bias,
+                     float *pre, void *y_bf16, float *y_f32, int gelu, int creal, void *stream);
+int lexgb_cnn_gelu_bwd(long long npts, int c, int cpad, const float *dy, const float *pre, void *g_bf16,
+                       void *stream);
+int lexgb_cnn_conv3d_dw(int nx, int ny, int nz, int cin, int cout, int gstride, const void *x, const void *g,
+                        float *dw, float *db, void *stream);
+int lexgb_cnn_adam(long long n, float *w, const float *gw, float *m, float *v, void *w_bf16, float lr, float beta1,
+                   float beta2, float eps, int step, void *stream);
+
 int lexgb_last_error(char *buf, size_t len);
 
 #ifdef __cplusplus

@@ -59,6 +59,11 @@ SIGNATURES = {
     "lexgb_step_vjp": (_I, [_P, _I, ctypes.POINTER(_P), ctypes.POINTER(_P), _I]),
     "lexgb_step_keep": (_I, [_P]),
     "lexgb_step_vjp_kept": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), _I]),
+    "lexgb_cnn_conv3d": (_I, [_I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
+    "lexgb_cnn_gelu_bwd": (_I, [ctypes.c_longlong, _I, _I, _P, _P, _P, _P]),
+    "lexgb_cnn_conv3d_dw": (_I, [_I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P]),
+    "lexgb_cnn_adam": (_I, [ctypes.c_longlong, _P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                            ctypes.c_float, _I, _P]),
     "lexgb_last_error": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
 }
 
