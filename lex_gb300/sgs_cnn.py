@@ -1,0 +1,203 @@
+"""Learned SGS correction: the 3-D CNN of the reference (simpleCNN, dl_models.py:19-30) on the
+library's BF16 tensor-core kernels, as a torch.autograd operation.
+
+    x (5 normalised fields at cell centres) -> conv 5->32, GELU -> conv 32->32, GELU
+      -> conv 32->32, GELU -> conv 32->5 -> correction (5 fields)
+
+All convolutions are 3x3x3 with zero padding ('SAME'), biases on, tanh-GELU (flax ``nn.gelu``).
+The forward runs ``lexgb_cnn_conv3d`` (BF16 operands, FP32 accumulation); the backward runs the
+same kernel on the mirrored, transposed weights for the input gradients, ``lexgb_cnn_gelu_bwd``
+and ``lexgb_cnn_conv3d_dw`` for the weight and bias gradients.  ``adam_step`` updates the FP32
+master weights with ``lexgb_cnn_adam`` (the reference uses optax.lamb, lex_dl_train.py).
+
+Packing (dl_models.py:125-182): theta, u, v, w, qv are min-max normalised with per-field
+scalars, the winds averaged to cell centres; the correction's winds go back to faces by the
+periodic average in x and y and by averaging to interior w faces (zero at the bottom and the
+lid).  The reference's stagger_uvw copies an interior face value to the periodic end faces; this
+module uses the periodic neighbour instead.  Packing runs as torch element-wise operations.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+
+CIN0, C, COUT_REAL = 5, 32, 5
+LAYERS = ((16, 32, True), (32, 32, True), (32, 32, True), (32, 8, False))  # (cin padded, cout padded, GELU)
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class SGSNet:
+    """Parameters (FP32 masters + BF16 copies) and Adam moments of the four convolutions."""
+
+    def __init__(self, seed=0, init_scale=1.0):
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        self.w, self.b, self.wbf = [], [], []
+        for li, (cin, cout, _) in enumerate(LAYERS):
+            rin = CIN0 if li == 0 else C
+            rout = COUT_REAL if li == 3 else C
+            w = torch.zeros(27, cout, cin)
+            std = init_scale * (2.0 / (27 * rin)) ** 0.5
+            w[:, :rout, :rin] = torch.randn(27, rout, rin, generator=g) * std
+            if li == 3:
+                w *= 0.1   # a small correction to start from
+            self.w.append(w.cuda())
+            self.b.append(torch.zeros(cout, device="cuda"))
+        self.m = [torch.zeros_like(t) for t in self.w + self.b]
+        self.v = [torch.zeros_like(t) for t in self.w + self.b]
+        self.step_count = 0
+        self.refresh()
+
+    def refresh(self):
+        self.wbf = [w.to(torch.bfloat16).contiguous() for w in self.w]
+
+    def params(self):
+        return self.w + self.b
+
+    def state_dict(self):
+        return {"w": [t.cpu() for t in self.w], "b": [t.cpu() for t in self.b]}
+
+    def load_state_dict(self, d):
+        self.w = [t.cuda() for t in d["w"]]
+        self.b = [t.cuda() for t in d["b"]]
+        self.refresh()
+
+
+def conv3d(x_bf16, w_bf16, bias, nx, ny, nz, cin, cout, gelu, creal, want_pre=True, out_f32=False):
+    """One convolution; x_bf16 [npts, cin] -> (pre FP32 or None, y BF16 or None, y FP32 or None)."""
+    n = nx * ny * nz
+    pre = torch.empty(n, cout, device="cuda") if want_pre else None
+    ybf = None if out_f32 else torch.empty(n, cout, device="cuda", dtype=torch.bfloat16)
+    yf = torch.empty(n, cout, device="cuda") if out_f32 else None
+    _lib.check(_lib.load().lexgb_cnn_conv3d(nx, ny, nz, cin, cout, _p(x_bf16), _p(w_bf16), _p(bias), _p(pre),
+                                            _p(ybf), _p(yf), 1 if gelu else 0, creal, _stream()))
+    return pre, ybf, yf
+
+
+def _mirror(w_bf16):
+    """[27][cout][cin] -> [27][cin][cout] with the offsets reversed: the input-gradient weights."""
+    return w_bf16.flip(0).transpose(1, 2).contiguous()
+
+
+def _pad_channels(t, c):
+    if t.shape[1] == c:
+        return t.contiguous()
+    out = torch.zeros(t.shape[0], c, device=t.device, dtype=t.dtype)
+    out[:, :t.shape[1]] = t
+    return out
+
+
+class _NetFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, net, dims, *params):
+        nx, ny, nz = dims
+        a = _pad_channels(x.to(torch.bfloat16), 16)
+        acts, pres = [a], []
+        for li, (cin, cout, gelu) in enumerate(LAYERS):
+            last = li == len(LAYERS) - 1
+            pre, ybf, yf = conv3d(acts[-1], net.wbf[li], net.b[li], nx, ny, nz, cin, cout, gelu,
+                                  COUT_REAL if last else cout, want_pre=not last, out_f32=last)
+            pres.append(pre)
+            if not last:
+                acts.append(ybf)
+            else:
+                out = yf[:, :COUT_REAL].contiguous()
+        ctx.net, ctx.dims, ctx.acts, ctx.pres = net, dims, acts, pres
+        return out
+
+    @staticmethod
+    def backward(ctx, gout):
+        net, (nx, ny, nz) = ctx.net, ctx.dims
+        lib = _lib.load()
+        n = nx * ny * nz
+        st = _stream()
+        # gradient at the last layer's output: no GELU; channels padded to 16 for the input-gradient conv
+        dy = _pad_channels(gout.float().contiguous(), 8)
+        g = torch.empty(n, 16, device="cuda", dtype=torch.bfloat16)
+        _lib.check(lib.lexgb_cnn_gelu_bwd(n, 8, 16, _p(dy), None, _p(g), st))
+        gstride = 16
+        grads_w = [None] * len(LAYERS)
+        grads_b = [None] * len(LAYERS)
+        dx = None
+        for li in range(len(LAYERS) - 1, -1, -1):
+            cin, cout, _ = LAYERS[li]
+            dw = torch.zeros(27, cout, cin, device="cuda")
+            db = torch.zeros(cout, device="cuda")
+            _lib.check(lib.lexgb_cnn_conv3d_dw(nx, ny, nz, cin, cout, gstride, _p(ctx.acts[li]), _p(g), _p(dw),
+                                               _p(db), st))
+            grads_w[li], grads_b[li] = dw, db
+            # input gradient: mirrored weights, padded so that the gradient's channels are the k16 input
+            wm = _mirror(net.wbf[li])                       # [27][cin][cout]
+            if gstride != cout:
+                wm = torch.cat([wm, torch.zeros(27, cin, gstride - cout, device="cuda", dtype=wm.dtype)], 2)
+            _, _, da = conv3d(g, wm.contiguous(), None, nx, ny, nz, gstride, cin, False, cin,
+                              want_pre=False, out_f32=True)
+            if li == 0:
+                dx = da[:, :CIN0].contiguous()
+                break
+            g = torch.empty(n, cin, device="cuda", dtype=torch.bfloat16)
+            _lib.check(lib.lexgb_cnn_gelu_bwd(n, cin, cin, _p(da), _p(ctx.pres[li - 1]), _p(g), st))
+            gstride = cin
+        return (dx, None, None) + tuple(grads_w) + tuple(grads_b)
+
+
+def net_apply(net, x, dims):
+    """Correction for x [npts, 5] (FP32, differentiable in x and the parameters)."""
+    return _NetFn.apply(x, net, dims, *net.params())
+
+
+def adam_step(net, grads, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+    """One Adam step of the network's FP32 master parameters on the GPU (lexgb_cnn_adam)."""
+    lib = _lib.load()
+    net.step_count += 1
+    for i, (p, gr) in enumerate(zip(net.params(), grads)):
+        if gr is None:
+            continue
+        gr = gr.contiguous().float()
+        _lib.check(lib.lexgb_cnn_adam(p.numel(), _p(p), _p(gr), _p(net.m[i]), _p(net.v[i]), None,
+                                      lr, beta1, beta2, eps, net.step_count, _stream()))
+    net.refresh()
+
+
+# ------------------------------------------------------------------------------------------------
+# packing of the device-layout state (theta, u, v, w, pi', qv) (dl_models.py:125-182)
+# ------------------------------------------------------------------------------------------------
+FIELDS5 = ("theta", "u", "v", "w", "qv")
+
+
+def pack(state, scale):
+    """state: six CUDA tensors (nz, ny, nx) / w (nz+1, ny, nx) -> [npts, 5] normalised, x fastest."""
+    th, u, v, w, _, q = state
+    ui = 0.5 * (u + torch.roll(u, -1, dims=2))
+    vi = 0.5 * (v + torch.roll(v, -1, dims=1))
+    wi = 0.5 * (w[:-1] + w[1:])
+    cols = []
+    for name, a in zip(FIELDS5, (th, ui, vi, wi, q)):
+        lo, hi = scale[name]
+        cols.append(((a - lo) / (hi - lo)).reshape(-1))
+    return torch.stack(cols, 1)
+
+
+def unpack(corr, scale, dims):
+    """[npts, 5] correction -> additions to (theta, u, v, w, pi', qv) on the staggered grid."""
+    nx, ny, nz = dims
+    f = [corr[:, i].reshape(nz, ny, nx) * (scale[n][1] - scale[n][0]) for i, n in enumerate(FIELDS5)]
+    th, ui, vi, wi, q = f
+    u = 0.5 * (ui + torch.roll(ui, 1, dims=2))
+    v = 0.5 * (vi + torch.roll(vi, 1, dims=1))
+    z = torch.zeros(1, ny, nx, device=corr.device)
+    w = torch.cat([z, 0.5 * (wi[:-1] + wi[1:]), z], 0)
+    return (th, u, v, w, torch.zeros_like(th), q)
+
+
+def correct(net, state, scale, dims):
+    """state + CNN correction (one_sprint_functions.py:128-163), differentiable."""
+    d = unpack(net_apply(net, pack(state, scale), dims), scale, dims)
+    return tuple(a + b for a, b in zip(state, d))

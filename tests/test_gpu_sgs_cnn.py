@@ -1,0 +1,78 @@
+"""The learned-SGS CNN kernels against a plain PyTorch fp32 reference of the same network
+(torch conv3d on the same BF16-rounded weights): forward, input and parameter gradients, Adam.
+Tolerances are BF16 level (activations are stored in BF16 between layers)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _reference(net, x, dims):
+    import torch
+    import torch.nn.functional as F
+    from lex_gb300.sgs_cnn import LAYERS
+    nx, ny, nz = dims
+    ws, bs = [], []
+    a = x.reshape(nz, ny, nx, -1).permute(3, 0, 1, 2).unsqueeze(0)     # [1, C, z, y, x]
+    a = a.to(torch.bfloat16).float()
+    for li, (cin, cout, gelu) in enumerate(LAYERS):
+        w = net.w[li].to(torch.bfloat16).float().detach().clone().requires_grad_(True)
+        b = net.b[li].detach().clone().requires_grad_(True)
+        ws.append(w)
+        bs.append(b)
+        wt = w.reshape(3, 3, 3, cout, cin).permute(3, 4, 0, 1, 2)         # [cout, cin, dz, dy, dx]
+        if a.shape[1] < cin:
+            a = torch.cat([a, torch.zeros(1, cin - a.shape[1], nz, ny, nx, device="cuda")], 1)
+        a = F.conv3d(a, wt, b, padding=1)
+        if gelu:
+            a = F.gelu(a, approximate="tanh")
+            a = a.to(torch.bfloat16).float()       # the kernels store activations in BF16
+    out = a[0, :5].permute(1, 2, 3, 0).reshape(-1, 5)
+    return out, ws, bs
+
+
+def _rel(a, b):
+    return float((a - b).norm() / b.norm())
+
+
+def test_cnn_forward_and_gradients_match_torch(built_lib):
+    torch = pytest.importorskip("torch")
+    from lex_gb300 import sgs_cnn
+    dims = (16, 8, 6)
+    n = dims[0] * dims[1] * dims[2]
+    net = sgs_cnn.SGSNet(seed=1, init_scale=1.0)
+    for t in net.params():
+        t.requires_grad_(True)
+    g = torch.Generator(device="cpu").manual_seed(2)
+    x = torch.rand(n, 5, generator=g).cuda().requires_grad_(True)
+    out = sgs_cnn.net_apply(net, x, dims)
+    xr = x.detach().clone().requires_grad_(True)
+    ref, ws, bs = _reference(net, xr, dims)
+    assert _rel(out.detach(), ref.detach()) < 2e-2
+    seed = torch.randn(n, 5, generator=g).cuda()
+    gx, *gp = torch.autograd.grad((out * seed).sum(), [x] + net.params())
+    rx, *rp = torch.autograd.grad((ref * seed).sum(), [xr] + ws + bs)
+    assert _rel(gx, rx) < 3e-2, _rel(gx, rx)
+    for i, (a, b) in enumerate(zip(gp, rp)):
+        if b.norm() > 0:
+            assert _rel(a, b) < 3e-2, (i, _rel(a, b))
+
+
+def test_adam_matches_formula(built_lib):
+    torch = pytest.importorskip("torch")
+    from lex_gb300 import sgs_cnn
+    net = sgs_cnn.SGSNet(seed=3)
+    w0 = [t.detach().clone() for t in net.params()]
+    m = [torch.zeros_like(t) for t in w0]
+    v = [torch.zeros_like(t) for t in w0]
+    g = torch.Generator(device="cpu").manual_seed(4)
+    lr, b1, b2, eps = 1e-3, 0.9, 0.999, 1e-8
+    for step in range(1, 4):
+        grads = [torch.randn(t.shape, generator=g).cuda() for t in w0]
+        sgs_cnn.adam_step(net, grads, lr, b1, b2, eps)
+        for i, gr in enumerate(grads):
+            m[i] = b1 * m[i] + (1 - b1) * gr
+            v[i] = b2 * v[i] + (1 - b2) * gr * gr
+            w0[i] = w0[i] - lr * (m[i] / (1 - b1 ** step)) / ((v[i] / (1 - b2 ** step)).sqrt() + eps)
+    for a, b in zip(net.params(), w0):
+        assert float((a - b).abs().max()) < 1e-6
