@@ -64,6 +64,7 @@ SIGNATURES = {
     "lexgb_cnn_conv3d_dw": (_I, [_I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P]),
     "lexgb_cnn_adam": (_I, [ctypes.c_longlong, _P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                             ctypes.c_float, _I, _P]),
+    "lexgb_set_sgs_net": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), _P, _P, _P, _I]),
     "lexgb_last_error": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
 }
 

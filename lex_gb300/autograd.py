@@ -42,7 +42,10 @@ def _ptrs(tensors):
 
 
 def _bind_stream(solver):
-    solver.set_stream(torch.cuda.current_stream().cuda_stream)
+    # torch's default stream has the handle 0, which the C ABI reads as "the context's own
+    # stream": name the legacy default stream explicitly (cudaStreamLegacy) instead
+    h = torch.cuda.current_stream().cuda_stream
+    solver.set_stream(h if h else 1)
 
 
 def set_state(solver, tensors):
@@ -67,7 +70,8 @@ class _Step(torch.autograd.Function):
         set_state(solver, state)
         _bind_stream(solver)
         _lib.check(solver.lib.lexgb_step_keep(solver.handle))
-        solver._kept_token = getattr(solver, "_kept_token", 0) + 1
+        solver._keep_count = getattr(solver, "_keep_count", 0) + 1
+        solver._kept_token = solver._keep_count
         ctx.token = solver._kept_token
         ctx.solver = solver
         ctx.save_for_backward(*state)

@@ -84,6 +84,13 @@ struct lexgb_ctx {
   // reverse mode: workspace of the recomputed step and the adjoint fields (allocated on first use)
   float* adj_arena = nullptr;
   bool adj_kept = false;  // the workspace holds a step kept by lexgb_step_keep
+  // learned SGS correction (allocated on first use): weights, biases, ranges, activations
+  char* sgs_arena = nullptr;
+  bool sgs_on = false;
+  void* sgs_w[4]{};
+  float* sgs_b[4]{};
+  float *sgs_lo = nullptr, *sgs_rin = nullptr, *sgs_rout = nullptr, *sgs_corr = nullptr;
+  void *sgs_x = nullptr, *sgs_a0 = nullptr, *sgs_a1 = nullptr;
   // graph of one big step
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -200,6 +207,33 @@ int run_step(lexgb_ctx* c) {
   CKS(run_stage(c, 0, c->A, c->A, c->B, nullptr, nullptr));
   CKS(run_stage(c, 1, c->A, c->B, c->C, nullptr, nullptr));
   CKS(run_stage(c, 2, c->A, c->C, c->A, nullptr, nullptr));
+  return LEXGB_OK;
+}
+
+// the learned SGS correction of the state in A: pack, four convolutions, unpack
+constexpr int SGS_CIN[4] = {16, 32, 32, 32}, SGS_COUT[4] = {32, 32, 32, 8};
+
+int run_sgs(lexgb_ctx* c) {
+  const Dims& d = c->d;
+  CK(launch_sgs_pack(d.nx, d.ny, d.nz, c->A.T, c->A.u, c->A.v, c->A.w, c->A.q, (float)c->theta_ref, c->sgs_lo,
+                     c->sgs_rin, c->sgs_x, c->stream));
+  const void* in[4] = {c->sgs_x, c->sgs_a0, c->sgs_a1, c->sgs_a0};
+  void* out[3] = {c->sgs_a0, c->sgs_a1, c->sgs_a0};
+  for (int l = 0; l < 4; ++l) {
+    const bool last = l == 3;
+    const int st = lexgb_cnn_conv3d(d.nx, d.ny, d.nz, SGS_CIN[l], SGS_COUT[l], in[l], c->sgs_w[l], c->sgs_b[l],
+                                    nullptr, last ? nullptr : out[l], last ? c->sgs_corr : nullptr, last ? 0 : 1,
+                                    last ? 5 : SGS_COUT[l], c->stream);
+    if (st != LEXGB_OK) return st;
+  }
+  CK(launch_sgs_unpack(d.nx, d.ny, d.nz, c->sgs_corr, c->sgs_rout, c->A.T, c->A.u, c->A.v, c->A.w, c->A.q,
+                       c->stream));
+  return LEXGB_OK;
+}
+
+int run_big_step(lexgb_ctx* c) {
+  CKS(run_step(c));
+  if (c->sgs_on) CKS(run_sgs(c));
   return LEXGB_OK;
 }
 
@@ -377,6 +411,7 @@ int lexgb_destroy(lexgb_ctx* c) {
   cudaFree(c->arena);
   cudaFree(c->rec_arena);
   cudaFree(c->adj_arena);
+  cudaFree(c->sgs_arena);
   cudaFree(c->base64);
   cudaFree(c->tab);
   cudaFree(c->stage);
@@ -473,14 +508,23 @@ int lexgb_step(lexgb_ctx* c, int nsteps, int use_graph) {
   if (nsteps < 0) return fail(LEXGB_ERR_ARG, "nsteps must be >= 0");
   c->recorded = false;
   if (!use_graph) {
-    for (int n = 0; n < nsteps; ++n) CKS(run_step(c));
+    for (int n = 0; n < nsteps; ++n) CKS(run_big_step(c));
     return LEXGB_OK;
   }
   if (!c->gexec) {
-    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    const int st = run_step(c);
+    // capture on the context's own stream (the legacy default stream cannot be captured); the
+    // graph is then launched on whichever stream is bound
+    cudaStream_t bound = c->stream;
+    c->stream = c->own_stream;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+      c->stream = bound;
+      return fail(LEXGB_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    }
+    const int st = run_big_step(c);
     cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    e = cudaStreamEndCapture(c->stream, &g);
+    c->stream = bound;
     if (st != LEXGB_OK) {
       if (g) cudaGraphDestroy(g);
       return st;
@@ -490,6 +534,73 @@ int lexgb_step(lexgb_ctx* c, int nsteps, int use_graph) {
     CK(cudaGraphInstantiate(&c->gexec, c->graph, 0));
   }
   for (int n = 0; n < nsteps; ++n) CK(cudaGraphLaunch(c->gexec, c->stream));
+  return LEXGB_OK;
+}
+
+int lexgb_set_sgs_net(lexgb_ctx* c, const void* const w[4], const float* const b[4], const float* in_lo,
+                      const float* in_range, const float* out_range, int enable) {
+  if (!c) return fail(LEXGB_ERR_ARG, "null context");
+  if (!enable) {
+    if (c->sgs_on) {
+      CK(cudaStreamSynchronize(c->stream));
+      drop_graph(c);
+    }
+    c->sgs_on = false;
+    return LEXGB_OK;
+  }
+  const Dims& d = c->d;
+  if (d.nx % 16) return fail(LEXGB_ERR_ARG, "lexgb_set_sgs_net: nx must be a multiple of 16");
+  if (!w || !b || !in_lo || !in_range || !out_range) return fail(LEXGB_ERR_ARG, "lexgb_set_sgs_net: null argument");
+  for (int l = 0; l < 4; ++l)
+    if (!w[l] || !b[l]) return fail(LEXGB_ERR_ARG, "lexgb_set_sgs_net: null weight or bias");
+  const size_t cells = (size_t)d.cells();
+  auto up = [](size_t n) { return (n + 255) & ~(size_t)255; };
+  size_t wbytes[4], off = 0;
+  size_t o_w[4], o_b[4];
+  for (int l = 0; l < 4; ++l) {
+    wbytes[l] = (size_t)27 * SGS_COUT[l] * SGS_CIN[l] * 2;
+    o_w[l] = off;
+    off += up(wbytes[l]);
+    o_b[l] = off;
+    off += up(SGS_COUT[l] * sizeof(float));
+  }
+  const size_t o_lo = off, o_rin = (off += up(5 * d.nz * sizeof(float))), o_rout = (off += up(5 * d.nz * sizeof(float)));
+  const size_t o_corr = (off += up(5 * cells * sizeof(float)));
+  const size_t o_x = (off += up(8 * cells * sizeof(float)));
+  const size_t o_a0 = (off += up(cells * 16 * 2));
+  const size_t o_a1 = (off += up(cells * 32 * 2));
+  off += up(cells * 32 * 2);
+  if (!c->sgs_arena) {
+    cudaError_t e = cudaMalloc(&c->sgs_arena, off);
+    if (e != cudaSuccess) {
+      c->sgs_arena = nullptr;
+      return fail(LEXGB_ERR_ALLOC, std::string("learned SGS buffers: ") + cudaGetErrorString(e));
+    }
+    char* a = c->sgs_arena;
+    for (int l = 0; l < 4; ++l) {
+      c->sgs_w[l] = a + o_w[l];
+      c->sgs_b[l] = (float*)(a + o_b[l]);
+    }
+    c->sgs_lo = (float*)(a + o_lo);
+    c->sgs_rin = (float*)(a + o_rin);
+    c->sgs_rout = (float*)(a + o_rout);
+    c->sgs_corr = (float*)(a + o_corr);
+    c->sgs_x = a + o_x;
+    c->sgs_a0 = a + o_a0;
+    c->sgs_a1 = a + o_a1;
+  }
+  for (int l = 0; l < 4; ++l) {
+    CK(cudaMemcpyAsync(c->sgs_w[l], w[l], wbytes[l], cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->sgs_b[l], b[l], SGS_COUT[l] * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+  }
+  CK(cudaMemcpyAsync(c->sgs_lo, in_lo, 5 * d.nz * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->sgs_rin, in_range, 5 * d.nz * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->sgs_rout, out_range, 5 * cells * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+  if (!c->sgs_on) {
+    CK(cudaStreamSynchronize(c->stream));
+    drop_graph(c);
+  }
+  c->sgs_on = true;
   return LEXGB_OK;
 }
 

@@ -17,6 +17,9 @@
 //                  points for one offset and adds its partial sums atomically
 //   k_bias_grad    db[co] = sum_p g[p][co]
 //   k_adam         Adam update of FP32 master weights and their BF16 copies
+//   k_sgs_pack     the network's input from the device-layout state (dl_models.py:125-155)
+//   k_sgs_unpack   the scaled, re-staggered correction added to the state
+//                  (one_sprint_functions.py:136-151)
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -184,7 +187,79 @@ __global__ void k_adam(long long n, float* __restrict__ w, const float* __restri
   w[t] = ww;
   if (wbf) wbf[t] = __float2bfloat16(ww);
 }
+
+// Input of the network, one thread per cell, 16 BF16 channels (32 bytes):
+//   (theta, ui, vi, wi, qv, 0 x 11), each (value - lo[f][k]) / rin[f][k]
+// with theta = T + theta_ref and the winds averaged to the cell centre (u, v periodic).  The
+// arithmetic is the element-wise sequence of the PyTorch packing of the same state, rounded
+// the same way (no contractions), so both give the same BF16 inputs.
+__global__ void k_sgs_pack(int nx, int ny, int nz, const float* __restrict__ T, const float* __restrict__ u,
+                           const float* __restrict__ v, const float* __restrict__ w, const float* __restrict__ q,
+                           float theta_ref, const float* __restrict__ lo, const float* __restrict__ rin,
+                           uint4* __restrict__ x16) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long plane = (long long)nx * ny;
+  if (t >= plane * nz) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
+  const long long tu = t - i + (i + 1 == nx ? 0 : i + 1);
+  const long long tv = t + (long long)((j + 1 == ny ? 0 : j + 1) - j) * nx;
+  float f[5];
+  f[0] = __fadd_rn(T[t], theta_ref);
+  f[1] = __fmul_rn(0.5f, __fadd_rn(u[t], u[tu]));
+  f[2] = __fmul_rn(0.5f, __fadd_rn(v[t], v[tv]));
+  f[3] = __fmul_rn(0.5f, __fadd_rn(w[t], w[t + plane]));
+  f[4] = q[t];
+  __nv_bfloat16 h[6];
+#pragma unroll
+  for (int c = 0; c < 5; ++c) h[c] = __float2bfloat16_rn(__fdiv_rn(__fsub_rn(f[c], lo[c * nz + k]), rin[c * nz + k]));
+  h[5] = __float2bfloat16_rn(0.f);
+  uint4 a, b = make_uint4(0u, 0u, 0u, 0u);
+  a.x = (uint32_t)__bfloat16_as_ushort(h[0]) | ((uint32_t)__bfloat16_as_ushort(h[1]) << 16);
+  a.y = (uint32_t)__bfloat16_as_ushort(h[2]) | ((uint32_t)__bfloat16_as_ushort(h[3]) << 16);
+  a.z = (uint32_t)__bfloat16_as_ushort(h[4]) | ((uint32_t)__bfloat16_as_ushort(h[5]) << 16);
+  a.w = 0u;
+  x16[2 * t] = a;
+  x16[2 * t + 1] = b;
+}
+
+// The correction corr[p][0..4] (FP32, 8 channels a point) times the output range rout[f][p],
+// back on the grid: theta and qv at the cell, u (v) at the west (south) face as the mean of the
+// two cells beside it (periodic), w at the interior faces 1..nz-1 as the mean of the cells below
+// and above (the bottom and lid faces are not corrected).  One thread per cell; it writes only
+// its own cell and its own west, south and bottom faces.
+__global__ void k_sgs_unpack(int nx, int ny, int nz, const float* __restrict__ corr, const float* __restrict__ rout,
+                             float* __restrict__ T, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+                             float* __restrict__ q) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long plane = (long long)nx * ny, cells = plane * nz;
+  if (t >= cells) return;
+  const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
+  auto c = [&](long long p, int f) { return __fmul_rn(corr[p * 8 + f], rout[f * cells + p]); };
+  const long long tu = t - i + (i == 0 ? nx - 1 : i - 1);
+  const long long tv = t + (long long)((j == 0 ? ny - 1 : j - 1) - j) * nx;
+  T[t] = __fadd_rn(T[t], c(t, 0));
+  u[t] = __fadd_rn(u[t], __fmul_rn(0.5f, __fadd_rn(c(t, 1), c(tu, 1))));
+  v[t] = __fadd_rn(v[t], __fmul_rn(0.5f, __fadd_rn(c(t, 2), c(tv, 2))));
+  if (k > 0) w[t] = __fadd_rn(w[t], __fmul_rn(0.5f, __fadd_rn(c(t - plane, 3), c(t, 3))));
+  q[t] = __fadd_rn(q[t], c(t, 4));
+}
 }  // namespace
+
+cudaError_t launch_sgs_pack(int nx, int ny, int nz, const float* T, const float* u, const float* v, const float* w,
+                            const float* q, float theta_ref, const float* lo, const float* rin, void* x16,
+                            cudaStream_t st) {
+  const long long n = (long long)nx * ny * nz;
+  k_sgs_pack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nx, ny, nz, T, u, v, w, q, theta_ref, lo, rin,
+                                                          (uint4*)x16);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sgs_unpack(int nx, int ny, int nz, const float* corr, const float* rout, float* T, float* u,
+                              float* v, float* w, float* q, cudaStream_t st) {
+  const long long n = (long long)nx * ny * nz;
+  k_sgs_unpack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nx, ny, nz, corr, rout, T, u, v, w, q);
+  return cudaGetLastError();
+}
 }  // namespace lexgb
 
 // ------------------------------------------------------------------------------------------------

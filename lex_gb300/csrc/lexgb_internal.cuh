@@ -300,6 +300,14 @@ cudaError_t launch_smag_a(const Dims&, const Phys&, const Cols&, State in, SmagT
 struct SgsOut { float *u, *v, *w, *T, *q; };
 cudaError_t launch_smag_b(const Dims&, const Phys&, const Cols&, State in, SmagTau tau, SgsOut out, cudaStream_t);
 
+// learned SGS correction: network input from the state (16 BF16 channels a cell) and the
+// correction (8 FP32 channels a cell, 5 used) scaled and added back to the state
+cudaError_t launch_sgs_pack(int nx, int ny, int nz, const float* T, const float* u, const float* v, const float* w,
+                            const float* q, float theta_ref, const float* lo, const float* rin, void* x16,
+                            cudaStream_t);
+cudaError_t launch_sgs_unpack(int nx, int ny, int nz, const float* corr, const float* rout, float* T, float* u,
+                              float* v, float* w, float* q, cudaStream_t);
+
 // layout conversion between the reference's padded [x][y][z] host layout and the device layout
 // kind: 0 scalar, 1 u, 2 v, 3 w
 cudaError_t launch_import_padded(const Dims&, const void* src, int src_f64, int kind, double offset, float* dst,

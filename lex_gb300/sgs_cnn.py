@@ -10,11 +10,17 @@ same kernel on the mirrored, transposed weights for the input gradients, ``lexgb
 and ``lexgb_cnn_conv3d_dw`` for the weight and bias gradients.  ``adam_step`` updates the FP32
 master weights with ``lexgb_cnn_adam`` (the reference uses optax.lamb, lex_dl_train.py).
 
-Packing (dl_models.py:125-182): theta, u, v, w, qv are min-max normalised with per-field
-scalars, the winds averaged to cell centres; the correction's winds go back to faces by the
-periodic average in x and y and by averaging to interior w faces (zero at the bottom and the
-lid).  The reference's stagger_uvw copies an interior face value to the periodic end faces; this
-module uses the periodic neighbour instead.  Packing runs as torch element-wise operations.
+Packing (dl_models.py:125-182): theta, u, v, w, qv are min-max normalised per level, the winds
+averaged to cell centres first; the correction is scaled by an output range per cell and its
+winds go back to faces by the periodic average in x and y and by averaging to interior w faces
+(zero at the bottom and the lid).  The reference normalises the staggered winds before averaging
+them and its stagger_uvw copies an interior face value to the periodic end faces; this module
+averages first and uses the periodic neighbour.  Packing runs as torch element-wise operations
+here (differentiable, for training) and as the kernels of ``lexgb_set_sgs_net`` inside the
+library's step (inference, :func:`attach`); both round the same way.
+
+A scale is a dict of CUDA tensors: ``lo`` and ``rin`` [5, nz] (input minimum and range per
+level) and ``rout`` [5, nz, ny, nx] (output range per cell), fields (theta, u, v, w, qv).
 """
 import ctypes
 
@@ -31,13 +37,16 @@ def _p(t):
 
 
 def _stream():
-    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    h = torch.cuda.current_stream().cuda_stream
+    return ctypes.c_void_p(h if h else 1)   # 1: cudaStreamLegacy (torch's default stream)
 
 
 class SGSNet:
     """Parameters (FP32 masters + BF16 copies) and Adam moments of the four convolutions."""
 
-    def __init__(self, seed=0, init_scale=1.0):
+    def __init__(self, seed=0, init_scale=1.0, zero_last=True):
+        """He-normal weights, zero biases; zero_last: the last layer starts at zero, so that
+        training starts from the uncorrected model."""
         g = torch.Generator(device="cpu").manual_seed(seed)
         self.w, self.b, self.wbf = [], [], []
         for li, (cin, cout, _) in enumerate(LAYERS):
@@ -46,8 +55,8 @@ class SGSNet:
             w = torch.zeros(27, cout, cin)
             std = init_scale * (2.0 / (27 * rin)) ** 0.5
             w[:, :rout, :rin] = torch.randn(27, rout, rin, generator=g) * std
-            if li == 3:
-                w *= 0.1   # a small correction to start from
+            if li == 3 and zero_last:
+                w.zero_()
             self.w.append(w.cuda())
             self.b.append(torch.zeros(cout, device="cuda"))
         self.m = [torch.zeros_like(t) for t in self.w + self.b]
@@ -178,17 +187,17 @@ def pack(state, scale):
     ui = 0.5 * (u + torch.roll(u, -1, dims=2))
     vi = 0.5 * (v + torch.roll(v, -1, dims=1))
     wi = 0.5 * (w[:-1] + w[1:])
+    lo, rin = scale["lo"], scale["rin"]
     cols = []
-    for name, a in zip(FIELDS5, (th, ui, vi, wi, q)):
-        lo, hi = scale[name]
-        cols.append(((a - lo) / (hi - lo)).reshape(-1))
+    for f, a in enumerate((th, ui, vi, wi, q)):
+        cols.append(((a - lo[f].view(-1, 1, 1)) / rin[f].view(-1, 1, 1)).reshape(-1))
     return torch.stack(cols, 1)
 
 
 def unpack(corr, scale, dims):
     """[npts, 5] correction -> additions to (theta, u, v, w, pi', qv) on the staggered grid."""
     nx, ny, nz = dims
-    f = [corr[:, i].reshape(nz, ny, nx) * (scale[n][1] - scale[n][0]) for i, n in enumerate(FIELDS5)]
+    f = [corr[:, i].reshape(nz, ny, nx) * scale["rout"][i] for i in range(5)]
     th, ui, vi, wi, q = f
     u = 0.5 * (ui + torch.roll(ui, 1, dims=2))
     v = 0.5 * (vi + torch.roll(vi, 1, dims=1))
@@ -201,3 +210,40 @@ def correct(net, state, scale, dims):
     """state + CNN correction (one_sprint_functions.py:128-163), differentiable."""
     d = unpack(net_apply(net, pack(state, scale), dims), scale, dims)
     return tuple(a + b for a, b in zip(state, d))
+
+
+def cell_fields(state):
+    """(theta, ui, vi, wi, qv) at cell centres: the quantities the scale's ranges describe."""
+    th, u, v, w, _, q = state
+    return (th, 0.5 * (u + torch.roll(u, -1, dims=2)), 0.5 * (v + torch.roll(v, -1, dims=1)), 0.5 * (w[:-1] + w[1:]), q)
+
+
+def make_scale(states, margins=(0.01, 0.01, 0.01, 0.01, 1.0e-5)):
+    """Per-level minimum and maximum over `states` (dataset_generation.py:80-90): input range
+    max - min + margin per level (dl_models.py:128-152), output range max - min per level."""
+    lo, hi = None, None
+    for st in states:
+        cf = torch.stack([a.amin(dim=(1, 2)) for a in cell_fields(st)])
+        cx = torch.stack([a.amax(dim=(1, 2)) for a in cell_fields(st)])
+        lo = cf if lo is None else torch.minimum(lo, cf)
+        hi = cx if hi is None else torch.maximum(hi, cx)
+    nz, ny, nx = states[0][0].shape
+    m = torch.tensor(margins, device=lo.device).view(5, 1)
+    rout = (hi - lo).view(5, nz, 1, 1).expand(5, nz, ny, nx).contiguous()
+    return {"lo": lo.contiguous(), "rin": (hi - lo + m).contiguous(), "rout": rout}
+
+
+def attach(solver, net, scale):
+    """Apply the network after every big step of ``solver.step`` inside the library's step graph
+    (lexgb_set_sgs_net); call again after the weights change.  ``attach(solver, None, None)``
+    turns the correction off."""
+    from .autograd import _bind_stream
+    lib = _lib.load()
+    _bind_stream(solver)
+    if net is None:
+        _lib.check(lib.lexgb_set_sgs_net(solver.handle, None, None, None, None, None, 0))
+        return
+    P4 = ctypes.c_void_p * 4
+    w = P4(*[t.data_ptr() for t in net.wbf])
+    b = P4(*[t.data_ptr() for t in net.b])
+    _lib.check(lib.lexgb_set_sgs_net(solver.handle, w, b, _p(scale["lo"]), _p(scale["rin"]), _p(scale["rout"]), 1))

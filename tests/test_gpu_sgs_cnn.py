@@ -40,7 +40,7 @@ def test_cnn_forward_and_gradients_match_torch(built_lib):
     from lex_gb300 import sgs_cnn
     dims = (16, 8, 6)
     n = dims[0] * dims[1] * dims[2]
-    net = sgs_cnn.SGSNet(seed=1, init_scale=1.0)
+    net = sgs_cnn.SGSNet(seed=1, init_scale=1.0, zero_last=False)
     for t in net.params():
         t.requires_grad_(True)
     g = torch.Generator(device="cpu").manual_seed(2)
