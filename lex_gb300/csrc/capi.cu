@@ -221,10 +221,11 @@ int run_sgs(lexgb_ctx* c) {
   void* out[3] = {c->sgs_a0, c->sgs_a1, c->sgs_a0};
   for (int l = 0; l < 4; ++l) {
     const bool last = l == 3;
-    const int st = lexgb_cnn_conv3d(d.nx, d.ny, d.nz, SGS_CIN[l], SGS_COUT[l], in[l], c->sgs_w[l], c->sgs_b[l],
-                                    nullptr, last ? nullptr : out[l], last ? c->sgs_corr : nullptr, last ? 0 : 1,
-                                    last ? 5 : SGS_COUT[l], c->stream);
-    if (st != LEXGB_OK) return st;
+    // programmatic dependents: the weights and biases are the context's copies, written only by
+    // lexgb_set_sgs_net, so each layer stages them while the previous kernel finishes
+    CK(launch_cnn_conv3d(d.nx, d.ny, d.nz, SGS_CIN[l], SGS_COUT[l], in[l], c->sgs_w[l], c->sgs_b[l], nullptr,
+                         last ? nullptr : out[l], last ? c->sgs_corr : nullptr, last ? 0 : 1, last ? 5 : SGS_COUT[l],
+                         c->stream, true));
   }
   CK(launch_sgs_unpack(d.nx, d.ny, d.nz, c->sgs_corr, c->sgs_rout, c->A.T, c->A.u, c->A.v, c->A.w, c->A.q,
                        c->stream));
@@ -596,6 +597,7 @@ int lexgb_set_sgs_net(lexgb_ctx* c, const void* const w[4], const float* const b
   CK(cudaMemcpyAsync(c->sgs_lo, in_lo, 5 * d.nz * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaMemcpyAsync(c->sgs_rin, in_range, 5 * d.nz * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
   CK(cudaMemcpyAsync(c->sgs_rout, out_range, 5 * cells * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+  CK(conv_prepare());
   if (!c->sgs_on) {
     CK(cudaStreamSynchronize(c->stream));
     drop_graph(c);

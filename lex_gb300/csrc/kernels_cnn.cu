@@ -33,6 +33,17 @@ __device__ __forceinline__ float gelu_tanh(float x) {
   const float k0 = 0.7978845608028654f;  // sqrt(2/pi)
   return 0.5f * x * (1.f + tanhf(k0 * (x + 0.044715f * x * x * x)));
 }
+// forward GELU with the hardware tanh (tanh.approx.f32, relative error about 2^-11, below the
+// BF16 precision the activations are stored in)
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float gelu_tanh_fast(float x) {
+  const float k0 = 0.7978845608028654f;  // sqrt(2/pi)
+  return 0.5f * x * (1.f + tanh_fast(k0 * (x + 0.044715f * x * x * x)));
+}
 __device__ __forceinline__ float gelu_tanh_grad(float x) {
   const float k0 = 0.7978845608028654f;
   const float u = k0 * (x + 0.044715f * x * x * x);
@@ -108,6 +119,186 @@ __global__ void __launch_bounds__(128) k_conv3d(int nx, int ny, int nz, int cin,
       if (co >= creal) v = 0.f;  // padding channels stay zero
       if (ybf) ybf[p * COUT + co] = __float2bfloat16(v);
       if (yf) yf[p * COUT + co] = v;
+    }
+  }
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const __nv_bfloat16* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x2(uint32_t (&r)[2], const __nv_bfloat16* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(a));
+}
+
+// programmatic dependent launch: let the next kernel of the stream start its prologue / wait
+// until the previous kernel has completed and its writes are visible (both no-ops for kernels
+// launched without the programmatic-serialisation attribute)
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// 16-byte asynchronous copy global -> shared; valid = false writes zeros (no bytes read)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(sa), "l"(gmem), "r"(valid ? 16 : 0));
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Shared-memory convolution (CIN 16 or 32, COUT 8, 16 or 32): a persistent block of 12 warps
+// stages the layer's weights once ([27][COUT][CIN + 8]: the 8 padding channels put the 16-byte
+// rows of an 8x8 matrix in distinct banks), then loops over tiles of 16 x 8 x 1 points (x, y, z),
+// staging each tile's input with its halo ([3][10][18][CIN + 8], zero outside the grid) by
+// cp.async.  Warp (d, r) takes the 9 offsets of the input plane z + d - 1 for rows y0 + r and
+// y0 + r + 4, 16 points each, and every output channel (one A fragment feeds COUT / 8 MMAs, one
+// B fragment two); fragments are read with ldmatrix.  The three planes' partial sums meet in
+// shared memory and are added in plane order.
+constexpr int CONV_RP = 4, CONV_MR = 2, CONV_TY = CONV_RP * CONV_MR, CONV_WARPS = 3 * CONV_RP;
+
+template <int CIN, int COUT>
+struct ConvSmem {
+  static constexpr int CP = CIN + 8;
+  static constexpr int NT = COUT / 8;
+  static constexpr int THREADS = 32 * CONV_WARPS;
+  static constexpr int W_ELEMS = 27 * COUT * CP;
+  static constexpr int A_BYTES = 3 * (CONV_TY + 2) * 18 * CP * 2;
+  static constexpr int PS = COUT + 4;                          // partial-sum row stride (floats)
+  static constexpr int P_BYTES = CONV_TY * 16 * PS * 4;         // [128 points][PS]
+  static constexpr size_t BYTES = (size_t)W_ELEMS * 2 + (A_BYTES > P_BYTES ? A_BYTES : P_BYTES);
+};
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(ConvSmem<CIN, COUT>::THREADS)
+    k_conv3d_smem(int nx, int ny, int nz, const __nv_bfloat16* __restrict__ x, const __nv_bfloat16* __restrict__ w,
+                  const float* __restrict__ bias, float* __restrict__ pre, __nv_bfloat16* __restrict__ ybf,
+                  float* __restrict__ yf, int gelu, int creal, int early_weights) {
+  using L = ConvSmem<CIN, COUT>;
+  constexpr int CP = L::CP, NT = L::NT, KC = CIN / 16, CH = CIN / 8;  // CH: 16-byte chunks a row
+  extern __shared__ __align__(16) __nv_bfloat16 conv_smem[];
+  __nv_bfloat16* Ws = conv_smem;
+  __nv_bfloat16* As = conv_smem + L::W_ELEMS;
+  float* Ps = reinterpret_cast<float*>(As);  // partial sums, after the tile's reads of As
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int dz = wid / CONV_RP, rp = wid % CONV_RP;
+  // early_weights: the weights are not written by the previous kernel of the stream, so their
+  // staging overlaps that kernel's tail (launched as a programmatic dependent); the input is
+  // read only after pdl_wait
+  pdl_launch_dependents();
+  if (!early_weights) pdl_wait();
+  for (int e = tid; e < 27 * COUT * CH; e += L::THREADS) {
+    const int row = e / CH, c = e % CH;
+    cp_async16(Ws + row * CP + c * 8, w + (long long)row * CIN + c * 8, true);
+  }
+  if (early_weights) pdl_wait();
+  const int tiles_x = nx / 16, tiles_y = (ny + CONV_TY - 1) / CONV_TY;
+  const long long ntiles = (long long)tiles_x * tiles_y * nz;
+  const int g = lane >> 2, t = lane & 3;
+  // ldmatrix row addresses: A (x4): matrix m = lane/8 -> rows (m & 1) * 8 + lane % 8, k half m >> 1
+  const int a_row = ((lane >> 3) & 1) * 8 + (lane & 7), a_k = (lane >> 4) * 8;
+  // B (x4, two n8 tiles): matrix m -> tile m >> 1, k half m & 1; (x2) matrix m -> k half m
+  const int b_row = (lane >> 4) * 8 + (lane & 7), b_k = ((lane >> 3) & 1) * 8;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int tx = (int)(tile % tiles_x), ty = (int)((tile / tiles_x) % tiles_y);
+    const int z = (int)(tile / ((long long)tiles_x * tiles_y));
+    const int x0 = tx * 16, y0 = ty * CONV_TY;
+    __syncthreads();  // the previous tile's reads of As / Ps are done
+    for (int e = tid; e < 3 * (CONV_TY + 2) * 18 * CH; e += L::THREADS) {
+      const int c = e % CH, q = e / CH;
+      const int hx = q % 18, hy = (q / 18) % (CONV_TY + 2), hz = q / (18 * (CONV_TY + 2));
+      const int xx = x0 + hx - 1, yy = y0 + hy - 1, zz = z + hz - 1;
+      const bool in = xx >= 0 && xx < nx && yy >= 0 && yy < ny && zz >= 0 && zz < nz;
+      cp_async16(As + q * CP + c * 8, in ? x + (((long long)zz * ny + yy) * nx + xx) * CIN + c * 8 : x, in);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const int ya = y0 + rp, yb = ya + CONV_RP;  // the warp's two rows
+    const bool plane = z + dz - 1 >= 0 && z + dz - 1 < nz;
+    float acc[CONV_MR][NT][4];
+#pragma unroll
+    for (int m = 0; m < CONV_MR; ++m)
+#pragma unroll
+      for (int n = 0; n < NT; ++n)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[m][n][q] = 0.f;
+    if (plane && ya < ny) {
+#pragma unroll 1
+      for (int dy = 0; dy < 3; ++dy) {
+        const bool ina = ya + dy - 1 >= 0 && ya + dy - 1 < ny, inb = yb + dy - 1 >= 0 && yb + dy - 1 < ny;
+        if (!ina && !inb) continue;
+        const __nv_bfloat16* arow = As + ((dz * (CONV_TY + 2) + rp + dy) * 18) * CP;
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) {
+          const __nv_bfloat16* wo = Ws + ((dz * 9 + dy * 3 + dx) * COUT) * CP;
+#pragma unroll
+          for (int kc = 0; kc < KC; ++kc) {
+            uint32_t a[CONV_MR][4];
+#pragma unroll
+            for (int m = 0; m < CONV_MR; ++m)
+              ldsm_x4(a[m], arow + (m * CONV_RP * 18 + dx + a_row) * CP + kc * 16 + a_k);
+            if constexpr (NT == 1) {
+              uint32_t b[2];
+              ldsm_x2(b, wo + (lane & 7) * CP + kc * 16 + ((lane >> 3) & 1) * 8);
+#pragma unroll
+              for (int m = 0; m < CONV_MR; ++m) mma_bf16(acc[m][0], a[m], b);
+            } else {
+#pragma unroll
+              for (int n2 = 0; n2 < NT / 2; ++n2) {
+                uint32_t b4[4];
+                ldsm_x4(b4, wo + (n2 * 16 + b_row) * CP + kc * 16 + b_k);
+                const uint32_t b0[2] = {b4[0], b4[1]}, b1[2] = {b4[2], b4[3]};
+#pragma unroll
+                for (int m = 0; m < CONV_MR; ++m) {
+                  mma_bf16(acc[m][2 * n2], a[m], b0);
+                  mma_bf16(acc[m][2 * n2 + 1], a[m], b1);
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();  // every warp is done with As: it becomes the partial sums [point][channel]
+    // planes added in order: plane 0 writes (zeros where it does not exist), 1 and 2 add
+    constexpr int PS = L::PS;
+#pragma unroll 1
+    for (int d = 0; d < 3; ++d) {
+      if (dz == d && (d == 0 || (plane && ya < ny))) {
+#pragma unroll
+        for (int m = 0; m < CONV_MR; ++m)
+#pragma unroll
+          for (int n = 0; n < NT; ++n)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              float2* pp = reinterpret_cast<float2*>(Ps + ((rp + m * CONV_RP) * 16 + g + 8 * h) * PS + n * 8 + 2 * t);
+              float2 v = make_float2(acc[m][n][2 * h], acc[m][n][2 * h + 1]);
+              if (d > 0) {
+                const float2 o = *pp;
+                v = make_float2(o.x + v.x, o.y + v.y);
+              }
+              *pp = v;
+            }
+      }
+      __syncthreads();
+    }
+    // epilogue over the whole block: channel pairs of the tile's 128 points
+    for (int e = tid; e < CONV_TY * 16 * (COUT / 2); e += L::THREADS) {
+      const int pt = e / (COUT / 2), co = (e % (COUT / 2)) * 2;
+      const int y = y0 + pt / 16;
+      if (y >= ny) continue;
+      const long long p = ((long long)z * ny + y) * nx + x0 + (pt % 16);
+      const float2 sum = *reinterpret_cast<const float2*>(Ps + pt * PS + co);
+      float v0 = sum.x + (bias ? bias[co] : 0.f), v1 = sum.y + (bias ? bias[co + 1] : 0.f);
+      if (pre) *reinterpret_cast<float2*>(pre + p * COUT + co) = make_float2(v0, v1);
+      if (gelu) {
+        v0 = gelu_tanh_fast(v0);
+        v1 = gelu_tanh_fast(v1);
+      }
+      if (co >= creal) v0 = 0.f;
+      if (co + 1 >= creal) v1 = 0.f;
+      if (ybf) *reinterpret_cast<__nv_bfloat162*>(ybf + p * COUT + co) = __floats2bfloat162_rn(v0, v1);
+      if (yf) *reinterpret_cast<float2*>(yf + p * COUT + co) = make_float2(v0, v1);
     }
   }
 }
@@ -197,6 +388,7 @@ __global__ void k_sgs_pack(int nx, int ny, int nz, const float* __restrict__ T, 
                            const float* __restrict__ v, const float* __restrict__ w, const float* __restrict__ q,
                            float theta_ref, const float* __restrict__ lo, const float* __restrict__ rin,
                            uint4* __restrict__ x16) {
+  pdl_launch_dependents();
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long plane = (long long)nx * ny;
   if (t >= plane * nz) return;
@@ -230,6 +422,7 @@ __global__ void k_sgs_pack(int nx, int ny, int nz, const float* __restrict__ T, 
 __global__ void k_sgs_unpack(int nx, int ny, int nz, const float* __restrict__ corr, const float* __restrict__ rout,
                              float* __restrict__ T, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
                              float* __restrict__ q) {
+  pdl_wait();
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long plane = (long long)nx * ny, cells = plane * nz;
   if (t >= cells) return;
@@ -245,6 +438,78 @@ __global__ void k_sgs_unpack(int nx, int ny, int nz, const float* __restrict__ c
 }
 }  // namespace
 
+// Persistent-grid size of k_conv3d_smem<CIN, COUT> (resident blocks on the device), set up once:
+// the dynamic shared-memory opt-in and the occupancy query are not stream operations, so they
+// run here (conv_prepare) before any graph capture.
+template <int CIN, int COUT>
+cudaError_t conv_grid(int* cap) {
+  static int grid_cap = 0;
+  if (!grid_cap) {
+    using L = ConvSmem<CIN, COUT>;
+    cudaError_t e =
+        cudaFuncSetAttribute(k_conv3d_smem<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::BYTES);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv3d_smem<CIN, COUT>, L::THREADS, L::BYTES)) !=
+        cudaSuccess)
+      return e;
+    grid_cap = sms * (per > 0 ? per : 1);
+  }
+  *cap = grid_cap;
+  return cudaSuccess;
+}
+
+// pdl: launch as a programmatic dependent of the previous kernel of the stream, staging the
+// weights before waiting for it (the caller guarantees that kernel does not write them)
+template <int CIN, int COUT>
+cudaError_t launch_conv_smem(int nx, int ny, int nz, const __nv_bfloat16* x, const __nv_bfloat16* w,
+                             const float* bias, float* pre, __nv_bfloat16* ybf, float* yf, int gelu, int creal,
+                             cudaStream_t st, bool pdl) {
+  int cap = 0;
+  cudaError_t e = conv_grid<CIN, COUT>(&cap);
+  if (e != cudaSuccess) return e;
+  const long long ntiles = (long long)(nx / 16) * ((ny + CONV_TY - 1) / CONV_TY) * nz;
+  using L = ConvSmem<CIN, COUT>;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(ntiles < cap ? ntiles : cap));
+  cfg.blockDim = dim3(L::THREADS);
+  cfg.dynamicSmemBytes = L::BYTES;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k_conv3d_smem<CIN, COUT>, nx, ny, nz, x, w, bias, pre, ybf, yf, gelu, creal,
+                            pdl ? 1 : 0);
+}
+
+cudaError_t launch_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const void* x, const void* w,
+                              const float* bias, float* pre, void* ybf, float* yf, int gelu, int creal,
+                              cudaStream_t st, bool pdl) {
+  if (!(cin == 16 || cin == 32) || !(cout == 8 || cout == 16 || cout == 32) || nx % 16) return cudaErrorInvalidValue;
+  const __nv_bfloat16* xb = (const __nv_bfloat16*)x;
+  const __nv_bfloat16* wb = (const __nv_bfloat16*)w;
+  __nv_bfloat16* yb = (__nv_bfloat16*)ybf;
+#define LEXGB_CONV(CI, CO) launch_conv_smem<CI, CO>(nx, ny, nz, xb, wb, bias, pre, yb, yf, gelu, creal, st, pdl)
+  if (cin == 16) return cout == 8 ? LEXGB_CONV(16, 8) : cout == 16 ? LEXGB_CONV(16, 16) : LEXGB_CONV(16, 32);
+  return cout == 8 ? LEXGB_CONV(32, 8) : cout == 16 ? LEXGB_CONV(32, 16) : LEXGB_CONV(32, 32);
+#undef LEXGB_CONV
+}
+
+cudaError_t conv_prepare() {
+  int cap;
+  cudaError_t e;
+  if ((e = conv_grid<16, 8>(&cap)) != cudaSuccess) return e;
+  if ((e = conv_grid<16, 16>(&cap)) != cudaSuccess) return e;
+  if ((e = conv_grid<16, 32>(&cap)) != cudaSuccess) return e;
+  if ((e = conv_grid<32, 8>(&cap)) != cudaSuccess) return e;
+  if ((e = conv_grid<32, 16>(&cap)) != cudaSuccess) return e;
+  return conv_grid<32, 32>(&cap);
+}
+
 cudaError_t launch_sgs_pack(int nx, int ny, int nz, const float* T, const float* u, const float* v, const float* w,
                             const float* q, float theta_ref, const float* lo, const float* rin, void* x16,
                             cudaStream_t st) {
@@ -257,8 +522,16 @@ cudaError_t launch_sgs_pack(int nx, int ny, int nz, const float* T, const float*
 cudaError_t launch_sgs_unpack(int nx, int ny, int nz, const float* corr, const float* rout, float* T, float* u,
                               float* v, float* w, float* q, cudaStream_t st) {
   const long long n = (long long)nx * ny * nz;
-  k_sgs_unpack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(nx, ny, nz, corr, rout, T, u, v, w, q);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)((n + 255) / 256));
+  cfg.blockDim = dim3(256);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_sgs_unpack, nx, ny, nz, corr, rout, T, u, v, w, q);
 }
 }  // namespace lexgb
 
@@ -295,6 +568,9 @@ extern "C" int lexgb_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const
   const __nv_bfloat16* xb = (const __nv_bfloat16*)x;
   const __nv_bfloat16* wb = (const __nv_bfloat16*)w;
   __nv_bfloat16* yb = (__nv_bfloat16*)y_bf16;
+  if (cin == 16 || cin == 32)
+    return cnn_status(launch_cnn_conv3d(nx, ny, nz, cin, cout, x, w, bias, pre, y_bf16, y_f32, gelu, creal, st, false),
+                      "lexgb_cnn_conv3d");
   if (cout == 8)
     k_conv3d<1><<<blocks, 128, 0, st>>>(nx, ny, nz, cin, xb, wb, bias, pre, yb, y_f32, gelu, creal);
   else if (cout == 16)

@@ -305,6 +305,12 @@ cudaError_t launch_smag_b(const Dims&, const Phys&, const Cols&, State in, SmagT
 cudaError_t launch_sgs_pack(int nx, int ny, int nz, const float* T, const float* u, const float* v, const float* w,
                             const float* q, float theta_ref, const float* lo, const float* rin, void* x16,
                             cudaStream_t);
+cudaError_t conv_prepare();  // one-time set-up of the CNN convolution kernels (outside graph capture)
+// one convolution (cin 16 or 32, cout 8, 16 or 32); pdl: launched as a programmatic dependent of
+// the previous kernel of the stream, which must not write w or bias
+cudaError_t launch_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const void* x, const void* w,
+                              const float* bias, float* pre, void* ybf, float* yf, int gelu, int creal,
+                              cudaStream_t st, bool pdl);
 cudaError_t launch_sgs_unpack(int nx, int ny, int nz, const float* corr, const float* rout, float* T, float* u,
                               float* v, float* w, float* q, cudaStream_t);
 
