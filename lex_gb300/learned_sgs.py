@@ -95,19 +95,22 @@ def loss_fn(state, truth, scale):
     return total
 
 
-def train(S, net, series, scale, steps_per_sprint=10, iters=200, lr=1e-4, warmup=50, seed=0, log=None):
-    """Adam on sprints drawn from the coarse-grained series (lists of snapshot tuples); the
-    learning rate rises linearly over the first `warmup` iterations."""
+def train(S, net, series, scale, steps_per_sprint=10, iters=200, lr=1e-4, warmup=50, sprints=1, seed=0, log=None):
+    """Adam on rollouts drawn from the coarse-grained series (lists of snapshot tuples): from a
+    snapshot, `sprints` sprints of `steps_per_sprint` corrected coarse steps, the loss summed over
+    the snapshots they end at.  The learning rate rises linearly over the first `warmup` steps."""
     rng = np.random.default_rng(seed)
     for t in net.params():
         t.requires_grad_(True)
     hist = []
     for it in range(iters):
         s = series[rng.integers(len(series))]
-        k = int(rng.integers(len(s) - 1))
-        x0 = tuple(a.detach() for a in s[k])
-        out = sprint(S, x0, steps_per_sprint, net, scale)
-        loss = loss_fn(out, s[k + 1], scale)
+        k = int(rng.integers(len(s) - sprints))
+        state = tuple(a.detach() for a in s[k])
+        loss = 0.0
+        for j in range(1, sprints + 1):
+            state = sprint(S, state, steps_per_sprint, net, scale)
+            loss = loss + loss_fn(state, s[k + j], scale)
         grads = torch.autograd.grad(loss, net.params())
         n = net.step_count + 1
         sgs_cnn.adam_step(net, [g.detach() for g in grads], lr=lr * min(1.0, n / max(1, warmup)))
@@ -148,19 +151,65 @@ def step_cost(S, state, net=None, scale=None, n=200):
     return e0.elapsed_time(e1) / n
 
 
-def experiment(train_amplitudes=(1.5, 2.0, 2.5), train_seeds=(1, 2), test=(2.0, 77), iters=600, lr=1e-4, log=print):
-    """Train on fine runs of the given amplitudes / seeds, evaluate on a held-out run."""
+def experiment(train_amplitudes=(1.5, 2.0, 2.5), train_seeds=(1, 2), val=(2.0, 33), test=(2.0, 77), iters=1500,
+               chunk=100, lr=3e-5, sprints=1, log=print):
+    """Train on fine runs of the given bubble amplitudes and noise seeds; after every `chunk`
+    iterations the coarse run of a validation case is scored (mean relative theta' error over its
+    snapshots) and the best weights are kept; they are then evaluated on a held-out test case."""
     t0 = time.time()
     series = [fine_truth(a, s) for a in train_amplitudes for s in train_seeds]
+    val_snaps = fine_truth(*val)
     held = fine_truth(*test)
     scale = field_scale([x for s in series for x in s])
     S = coarse_solver()
+    base_val = theta_error(S, val_snaps)
     base = theta_error(S, held)
     net = sgs_cnn.SGSNet(seed=0)
-    hist = train(S, net, series, scale, iters=iters, lr=lr, log=log)
-    learned = theta_error(S, held, net, scale)
+    best = (float(np.mean(base_val)), None, 0)
+    curve = []
+    for c in range(max(1, iters // chunk)):
+        hist = train(S, net, series, scale, iters=chunk, lr=lr, sprints=sprints, seed=c)
+        v = float(np.mean(theta_error(S, val_snaps, net, scale)))
+        curve.append({"iters": (c + 1) * chunk, "loss": float(np.mean(hist)), "val_theta_err": v})
+        if log:
+            log("iters %d  mean loss %.4g  validation theta' error %.4f (Smagorinsky %.4f)"
+                % ((c + 1) * chunk, np.mean(hist), v, np.mean(base_val)))
+        if v < best[0]:
+            best = (v, net.state_dict(), (c + 1) * chunk)
+    if best[1] is not None:
+        net.load_state_dict(best[1])
+    learned = theta_error(S, held, net, scale) if best[1] is not None else list(base)
     cost_plain = step_cost(S, held[0])
     cost_learned = step_cost(S, held[0], net, scale)
-    return {"theta_err_smagorinsky": base, "theta_err_learned": learned, "loss_first": hist[:5],
-            "loss_last": hist[-5:], "ms_per_step_plain": cost_plain, "ms_per_step_learned": cost_learned,
-            "cost_ratio": cost_learned / cost_plain, "seconds": time.time() - t0, "net": net, "scale": scale}
+    S.close()
+    return {"theta_err_smagorinsky": base, "theta_err_learned": learned, "best_iters": best[2],
+            "val_theta_err_smagorinsky": float(np.mean(base_val)), "val_theta_err_learned": best[0], "curve": curve,
+            "ms_per_step_plain": cost_plain, "ms_per_step_learned": cost_learned,
+            "cost_ratio": cost_learned / cost_plain, "lr": lr, "sprints": sprints, "seconds": time.time() - t0,
+            "net": net, "scale": scale}
+
+
+def main(argv=None):
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="train and evaluate the learned SGS correction (warm bubble, "
+                                             "100 m fine runs coarse-grained to 600 m x 600 m x 300 m)")
+    ap.add_argument("--iters", type=int, default=1500)
+    ap.add_argument("--chunk", type=int, default=100)
+    ap.add_argument("--lr", type=float, default=3e-5)
+    ap.add_argument("--sprints", type=int, default=1)
+    ap.add_argument("--out", default=None, help="JSON summary; the weights go beside it (.pt)")
+    a = ap.parse_args(argv)
+    r = experiment(iters=a.iters, chunk=a.chunk, lr=a.lr, sprints=a.sprints)
+    net, scale = r.pop("net"), r.pop("scale")
+    line = json.dumps(r)
+    print(line)
+    if a.out:
+        with open(a.out, "w") as f:
+            f.write(line + "\n")
+        torch.save({"net": net.state_dict(), "scale": {k: v.cpu() for k, v in scale.items()}},
+                   a.out.rsplit(".", 1)[0] + ".pt")
+
+
+if __name__ == "__main__":
+    main()
