@@ -324,6 +324,26 @@ def run_lexgb(args):
                    "note": "forward_plus_adjoint: lexgb_step_keep + lexgb_step_vjp_kept (intermediates kept by "
                            "the forward); checkpointed: graph forward + lexgb_step_vjp, which recomputes the "
                            "step; xbar finite: %s" % bool(all(torch.isfinite(t).all().item() for t in xbar))}
+    # ---- learned SGS correction fused into the coarse step (600 m x 600 m x 300 m, 32^3, dt = 3 s)
+    sgs = None
+    if not args.no_sgs:
+        from lex_gb300 import learned_sgs as lsgs, sgs_cnn, autograd as lag
+        from lex_gb300.workload import warm_bubble
+        Sc = lsgs.coarse_solver(dims=(32, 32, 32))
+        cphys, _ = warm_bubble(32, 32, 32, 600.0, 600.0, 300.0)
+        Sc.upload(cphys, dtype=np.float32)
+        Sc.step(20)
+        xc = lag.get_state(Sc)
+        net = sgs_cnn.SGSNet(seed=0, zero_last=False)
+        net.w[3] *= 0.01   # corrections of the size a trained network makes
+        net.refresh()
+        cplain = lsgs.step_cost(Sc, xc, n=300)
+        clearn = lsgs.step_cost(Sc, xc, net, sgs_cnn.make_scale([xc]), n=300)
+        Sc.close()
+        sgs = {"grid": [32, 32, 32], "dx_m": [600.0, 600.0, 300.0], "dt_s": 3.0,
+               "ms_per_step_plain": cplain, "ms_per_step_learned": clearn, "cost_ratio": clearn / cplain,
+               "note": "CNN 5-32-32-32-5 (3x3x3, BF16 tensor cores) applied after every big step inside the "
+                       "step's CUDA graph (lexgb_set_sgs_net); CUDA events over 300 steps each"}
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -353,12 +373,36 @@ def run_lexgb(args):
     }
     if adjoint is not None:
         line["adjoint"] = adjoint
+    if sgs is not None:
+        line["learned_sgs"] = sgs
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line), flush=True)
     S.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def profile_sgs(args):
+    """Warm-up + timed coarse steps (32^3, 600 m x 600 m x 300 m) with the fused CNN correction."""
+    import torch
+    from lex_gb300 import learned_sgs as lsgs, sgs_cnn, autograd as lag
+    from lex_gb300.workload import warm_bubble
+    S = lsgs.coarse_solver(dims=(32, 32, 32))
+    phys, _ = warm_bubble(32, 32, 32, 600.0, 600.0, 300.0)
+    S.upload(phys, dtype=np.float32)
+    S.step(args.warmup)
+    x = lag.get_state(S)
+    net = sgs_cnn.SGSNet(seed=0, zero_last=False)
+    net.w[3] *= 0.01
+    net.refresh()
+    sgs_cnn.attach(S, net, sgs_cnn.make_scale([x]))
+    S.step(args.warmup)
+    torch.cuda.synchronize()
+    S.step(args.steps)
+    torch.cuda.synchronize()
+    S.close()
+    print(json.dumps({"profile_sgs": True, "steps": args.steps, "warmup": args.warmup}))
 
 
 def main():
@@ -369,11 +413,16 @@ def main():
     ap.add_argument("--impl", default="lexgb", choices=["lexgb", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the forward+adjoint cost measurement")
+    ap.add_argument("--no-sgs", action="store_true", help="skip the learned-SGS step cost measurement")
     ap.add_argument("--profile", action="store_true", help="only warm-up + timed steps (profiler captures)")
+    ap.add_argument("--profile-sgs", action="store_true",
+                    help="only a few coarse 32^3 steps with the fused learned SGS correction (profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "lexgb":
         args.warmup = 3
-    if args.impl == "reference":
+    if args.profile_sgs:
+        profile_sgs(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_lexgb(args)
