@@ -5,6 +5,8 @@ LEX's driver imports this module's names (``lex_relay.py:11``) and calls
     get_first_step_flux(phys_state, base_state, grids, model_opt)      lex_relay.py:25
     ws_rk3_sprint(phys_state, base_state, grids, model_opt)            lex_relay.py:48
     ws_rk3_big_step(phys_state, base_state, grids, model_opt)          one_sprint_functions.py:10-30
+    ws_rk3_sprint_dl(phys_state, base_state, grids, model_opt,
+                     dl_params, scaling_params)                        lex_dl_relay.py:97
 
 with the tuples of ``setup_lex.setup_grid_n_ic`` (setup_lex.py:66-69):
 
@@ -30,16 +32,17 @@ _nl = None
 _solver = None
 _key = None
 _last = None   # (returned tuple, id of its arrays) of the last sprint
+_sgs = None    # (ids of dl_params and scaling_params, device tensors) of the attached network
 
 
 def configure(namelist):
     """Use ``namelist`` (any object with nx, ny, nz, dx, dy, dz, dt, n_sound, sprint_n and,
     when cor_opt is on, fCor) instead of importing ``namelist_n_constants``."""
-    global _nl, _solver, _key, _last
+    global _nl, _solver, _key, _last, _sgs
     _nl = namelist
     if _solver is not None:
         _solver.close()
-    _solver, _key, _last = None, None, None
+    _solver, _key, _last, _sgs = None, None, None, None
 
 
 def _namelist():
@@ -67,7 +70,7 @@ def check_model_opt(model_opt):
 
 
 def _ensure(base_state, model_opt):
-    global _solver, _key, _last
+    global _solver, _key, _last, _sgs
     nl = _namelist()
     cor_opt, turb_opt = check_model_opt(model_opt)
     key = (int(nl.nx), int(nl.ny), int(nl.nz), float(nl.dx), float(nl.dy), float(nl.dz), float(nl.dt),
@@ -78,7 +81,7 @@ def _ensure(base_state, model_opt):
         _solver = Solver(key[0], key[1], key[2], key[3], key[4], key[5], key[6], key[7], turb_opt=turb_opt,
                          cor_opt=cor_opt, f_cor=key[10])
         _solver._base_cols = None
-        _key, _last = key, None
+        _key, _last, _sgs = key, None, None
     # the device stores theta relative to theta0 of the base state: a new base state also
     # invalidates the resident phys_state
     cols = tuple(np.asarray(base_state[i], dtype=np.float64)[0, 0, :].copy() for i in (2, 4, 3, 1))
@@ -96,9 +99,10 @@ def _sfc_zeros():
     return (-999, -999, z(), z(), z(), z(), z(), z(), z())
 
 
-def _advance(phys_state, base_state, model_opt, nsteps):
+def _advance(phys_state, base_state, model_opt, nsteps, sgs=None):
     global _last
     s = _ensure(base_state, model_opt)
+    _attach(s, sgs)
     resident = _last is not None and len(phys_state) == 6 and all(a is b for a, b in zip(phys_state, _last))
     if not resident:
         s.upload(tuple(np.asarray(a) for a in phys_state))
@@ -109,6 +113,77 @@ def _advance(phys_state, base_state, model_opt, nsteps):
     return out
 
 
+def _sgs_tensors(dl_params, scaling_params, nx, ny, nz):
+    """The reference's simpleCNN parameters and scaling_params as the library's device tensors.
+
+    dl_params: {'Conv_0' .. 'Conv_3': {'kernel': [3, 3, 3, cin, cout] (x, y, z offsets), 'bias':
+    [cout]}} (dl_models.py:19-30, flax: cross-correlation, zero padding) -> BF16 [27][cout][cin]
+    with the offset (dz+1)*9 + (dy+1)*3 + (dx+1), channels zero-padded to the kernels' widths.
+    scaling_params: (theta_min, theta_max, u_min, u_max, v_min, v_max, w_min, w_max, qv_min,
+    qv_max, ...) with keepdims shapes (dataset_generation.py:80-105).  Input: per-level minimum
+    and max - min + 0.01 (1e-5 for qv) over x and y (dl_models.py:128-152); output: the per-cell
+    max - min (one_sprint_functions.py:139-143).  Where the reference's ranges live on faces
+    (u, v, w), the two faces of a cell are averaged, because the library scales the cell-centred
+    correction before staggering it."""
+    import torch
+    from . import sgs_cnn
+    ws, bs = [], []
+    for li, (cin, cout, _) in enumerate(sgs_cnn.LAYERS):
+        p = dl_params["Conv_%d" % li]
+        k = np.asarray(p["kernel"], dtype=np.float32)
+        if k.ndim != 5 or k.shape[:3] != (3, 3, 3) or k.shape[3] > cin or k.shape[4] > cout:
+            raise ValueError("Conv_%d kernel must be [3, 3, 3, cin, cout] of simpleCNN, got %s" % (li, k.shape))
+        w = np.zeros((27, cout, cin), np.float32)
+        w[:, :k.shape[4], :k.shape[3]] = k.transpose(2, 1, 0, 4, 3).reshape(27, k.shape[4], k.shape[3])
+        b = np.zeros(cout, np.float32)
+        b[:k.shape[4]] = np.asarray(p["bias"], np.float32)
+        ws.append(torch.tensor(w).to(torch.bfloat16).cuda())
+        bs.append(torch.tensor(b).cuda())
+    if len(scaling_params) < 10:
+        raise ValueError("scaling_params must hold (theta, u, v, w, qv) minima and maxima")
+    lo, rin, rout = [], [], []
+    for f, margin in enumerate((0.01, 0.01, 0.01, 0.01, 1.0e-5)):
+        mn = np.asarray(scaling_params[2 * f], np.float64).squeeze()
+        mx = np.asarray(scaling_params[2 * f + 1], np.float64).squeeze()
+        l, h = mn.min(axis=(0, 1)), mx.max(axis=(0, 1))
+        r = mx - mn
+        if f == 3 and l.size == nz + 1:       # w on faces
+            l, h = 0.5 * (l[:-1] + l[1:]), 0.5 * (h[:-1] + h[1:])
+            r = 0.5 * (r[:, :, :-1] + r[:, :, 1:])
+        if f == 1 and r.shape[0] == nx + 1:
+            r = 0.5 * (r[:-1] + r[1:])
+        if f == 2 and r.shape[1] == ny + 1:
+            r = 0.5 * (r[:, :-1] + r[:, 1:])
+        if l.shape != (nz,) or r.shape != (nx, ny, nz):
+            raise ValueError("scaling_params[%d:%d] do not match the grid" % (2 * f, 2 * f + 2))
+        lo.append(l)
+        rin.append(h - l + margin)
+        rout.append(r.transpose(2, 1, 0))
+    dev = lambda a: torch.tensor(np.ascontiguousarray(np.stack(a)), dtype=torch.float32).cuda()
+    return ws, bs, {"lo": dev(lo), "rin": dev(rin), "rout": dev(rout)}
+
+
+def _attach(solver, sgs):
+    """Attach (sgs = (dl_params, scaling_params)) or detach (None) the fused correction."""
+    global _sgs
+    from . import sgs_cnn
+    if sgs is None:
+        if _sgs is not None:
+            sgs_cnn.attach(solver, None, None)
+            _sgs = None
+        return
+    key = (id(sgs[0]), id(sgs[1]), id(solver))
+    if _sgs is not None and _sgs[0] == key:
+        return
+    nl = _namelist()
+    ws, bs, scale = _sgs_tensors(sgs[0], sgs[1], int(nl.nx), int(nl.ny), int(nl.nz))
+
+    class _Net:
+        wbf, b = ws, bs
+    sgs_cnn.attach(solver, _Net, scale)
+    _sgs = (key, ws, bs, scale)
+
+
 def ws_rk3_big_step(phys_state, base_state, grids, model_opt):
     """One WS-RK3 big step (one_sprint_functions.py:10-30) -> (phys_state, sfc_others)."""
     return _advance(phys_state, base_state, model_opt, 1), _sfc_zeros()
@@ -117,6 +192,15 @@ def ws_rk3_big_step(phys_state, base_state, grids, model_opt):
 def ws_rk3_sprint(phys_state, base_state, grids, model_opt):
     """nl.sprint_n big steps (one_sprint_functions.py:109-115) -> (phys_state, sfc_others)."""
     return _advance(phys_state, base_state, model_opt, int(_namelist().sprint_n)), _sfc_zeros()
+
+
+def ws_rk3_sprint_dl(phys_state, base_state, grids, model_opt, dl_params, scaling_params):
+    """nl.sprint_n big steps, each followed by the simpleCNN correction of theta, u, v, w, qv
+    (one_sprint_functions.py:118-163), applied by the library inside its step graph (BF16
+    tensor-core convolutions) -> (phys_state, sfc_others).  Needs nx a multiple of 16.  The
+    weights and ranges are uploaded again only when other parameter objects are passed."""
+    n = int(_namelist().sprint_n)
+    return _advance(phys_state, base_state, model_opt, n, sgs=(dl_params, scaling_params)), _sfc_zeros()
 
 
 def get_first_step_flux(phys_state, base_state, grids, model_opt):

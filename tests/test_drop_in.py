@@ -65,3 +65,73 @@ def test_big_step_and_sprint_match_reference(built_lib):
     for f, a, a0 in zip(FIELDS, x3, x0):
         assert state_err(a, g["f64_step3_" + f], a0, f) <= 1e-5, f
     sp.configure(namelist(g))                            # releases the solver
+
+
+def _flax_params(seed, scale=0.05):
+    """Random simpleCNN parameters in flax's layout: kernel [3, 3, 3, cin, cout] over (x, y, z)."""
+    rng = np.random.default_rng(seed)
+    p = {}
+    for li, (cin, cout) in enumerate([(5, 32), (32, 32), (32, 32), (32, 5)]):
+        p["Conv_%d" % li] = {"kernel": rng.normal(0, (2.0 / (27 * cin)) ** 0.5, (3, 3, 3, cin, cout)) *
+                             (scale if li == 3 else 1.0), "bias": rng.normal(0, 0.01, cout)}
+    return p
+
+
+def _flax_conv(x, k, b):
+    """flax nn.Conv (cross-correlation, zero 'SAME' padding) on x [X][Y][Z][cin], float64."""
+    X, Y, Z, _ = x.shape
+    xp = np.pad(x, ((1, 1), (1, 1), (1, 1), (0, 0)))
+    out = np.zeros((X, Y, Z, k.shape[4])) + b
+    for a in range(3):
+        for c in range(3):
+            for e in range(3):
+                out += np.einsum("xyzi,io->xyzo", xp[a:a + X, c:c + Y, e:e + Z], k[a, c, e])
+    return out
+
+
+def test_flax_kernels_convert_to_the_library_layout():
+    torch = pytest.importorskip("torch")
+    from lex_gb300 import one_sprint_functions as sp
+    k = _flax_params(3)["Conv_1"]["kernel"][:, :, :, :16, :8]
+    # the conversion of _sgs_tensors, on the CPU
+    w = k.transpose(2, 1, 0, 4, 3).reshape(27, 8, 16)
+    x = np.random.default_rng(4).normal(size=(6, 5, 4, 16))        # [x][y][z][c]
+    ref = _flax_conv(x, k, np.zeros(8))
+    # the library's convolution: device layout [z][y][x][c], weights [27][cout][cin] with the
+    # offset (dz+1)*9 + (dy+1)*3 + (dx+1), as torch conv3d over (z, y, x)
+    wt = torch.tensor(w).reshape(3, 3, 3, 8, 16).permute(3, 4, 0, 1, 2)
+    xt = torch.tensor(x.transpose(2, 1, 0, 3)).permute(3, 0, 1, 2).unsqueeze(0)
+    out = torch.nn.functional.conv3d(xt, wt, padding=1)[0].permute(3, 2, 1, 0).numpy()
+    assert np.abs(out - ref).max() < 1e-10
+    assert callable(sp.ws_rk3_sprint_dl)
+
+
+@pytest.mark.gpu
+def test_sprint_dl_applies_the_correction_inside_the_step(built_lib):
+    import torch
+    from lex_gb300 import one_sprint_functions as sp
+    g = load_golden("bubble_steps.npz")
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    assert nx % 16 == 0
+    x0 = tuple(g["in_" + f].copy() for f in FIELDS)
+    base = base_state(g)
+    sp.configure(namelist(g, sprint_n=2))
+    plain, _ = sp.ws_rk3_sprint(x0, base, None, OK)
+    # scaling_params with keepdims shapes; ranges from the input state's interior
+    inner = lambda a, ex=(0, 0, 0): a[3:3 + nx + ex[0], 3:3 + ny + ex[1], 1:1 + nz + ex[2]][None, None]
+    sc = []
+    for a, ex in zip((x0[0], x0[1], x0[2], x0[3], x0[5]), ((0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (0, 0, 0))):
+        sc += [inner(a, ex) - 0.5, inner(a, ex) + 0.5]
+    zero = _flax_params(5, scale=0.0)
+    for li in range(4):
+        zero["Conv_%d" % li]["bias"][:] = 0.0
+    same, _ = sp.ws_rk3_sprint_dl(x0, base, None, OK, zero, tuple(sc))
+    for a, b in zip(same, plain):                  # a zero network changes nothing
+        assert np.array_equal(a, b)
+    corr, _ = sp.ws_rk3_sprint_dl(x0, base, None, OK, _flax_params(5), tuple(sc))
+    d = [float(np.abs(a - b).max()) for a, b in zip(corr, plain)]
+    assert all(np.isfinite(a).all() for a in corr)
+    assert d[0] > 0 and d[1] > 0 and d[3] > 0 and d[5] > 0 and d[4] == 0.0, d   # pi' is not corrected
+    again, _ = sp.ws_rk3_sprint(x0, base, None, OK)    # the plain sprint detaches the network
+    for a, b in zip(again, plain):
+        assert np.array_equal(a, b)
