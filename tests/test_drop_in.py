@@ -115,7 +115,7 @@ def test_sprint_dl_applies_the_correction_inside_the_step(built_lib):
     assert nx % 16 == 0
     x0 = tuple(g["in_" + f].copy() for f in FIELDS)
     base = base_state(g)
-    sp.configure(namelist(g, sprint_n=2))
+    sp.configure(namelist(g, sprint_n=1))            # one corrected step: pi' stays the plain step's
     plain, _ = sp.ws_rk3_sprint(x0, base, None, OK)
     # scaling_params with keepdims shapes; ranges from the input state's interior
     inner = lambda a, ex=(0, 0, 0): a[3:3 + nx + ex[0], 3:3 + ny + ex[1], 1:1 + nz + ex[2]][None, None]
