@@ -53,3 +53,49 @@ def warm_bubble(nx, ny, nz, dx, dy, dz, amplitude=2.0, radius_h=2000.0, radius_v
     phys = (theta, np.zeros((shp[0] + 1, shp[1], shp[2])), np.zeros((shp[0], shp[1] + 1, shp[2])),
             np.zeros((shp[0], shp[1], shp[2] + 1)), np.zeros(shp), qv)
     return phys, {"theta0": theta0, "qv0": qv0}
+
+
+def warm_bubbles(nx, ny, nz, dx, dy, dz, bubbles, radius_v=1500.0, z_center=1500.0, theta_base=300.0,
+                 qv_surface=0.014, qv_scale_height=2500.0, noise=0.01, seed=2025):
+    """Several warm bubbles on the base state of warm_bubble: ``bubbles`` is a list of
+    (amplitude K, horizontal radius m, x centre m, y centre m); perturbations add.  Returns
+    (phys_state, profile) like warm_bubble."""
+    z = level_heights(nz, dz)
+    theta0 = np.full(z.shape, float(theta_base))
+    qv0 = qv_surface * np.exp(-z / qv_scale_height)
+    X, Y, Z = np.meshgrid((np.arange(nx) + 0.5) * dx, (np.arange(ny) + 0.5) * dy, z[NGZ:-NGZ], indexing="ij")
+    dtheta = np.zeros(X.shape)
+    for amp, rh, xc, yc in bubbles:
+        r = np.sqrt(((X - xc) / rh) ** 2 + ((Y - yc) / rh) ** 2 + ((Z - z_center) / radius_v) ** 2)
+        dtheta += np.where(r <= 1.0, amp * np.cos(0.5 * np.pi * r) ** 2, 0.0)
+    if noise:
+        dtheta = dtheta + np.random.default_rng(seed).uniform(-noise, noise, size=dtheta.shape)
+    theta = _pad(theta0[NGZ:-NGZ][None, None, :] + dtheta, "s")
+    qv = _pad(np.broadcast_to(qv0[NGZ:-NGZ], dtheta.shape).copy(), "s")
+    shp = (nx + 2 * NGX, ny + 2 * NGY, nz + 2 * NGZ)
+    phys = (theta, np.zeros((shp[0] + 1, shp[1], shp[2])), np.zeros((shp[0], shp[1] + 1, shp[2])),
+            np.zeros((shp[0], shp[1], shp[2] + 1)), np.zeros(shp), qv)
+    return phys, {"theta0": theta0, "qv0": qv0}
+
+
+def random_bubbles(seed, n, lx, ly, amplitude=(1.0, 3.0), radius=(1500.0, 3000.0), centred=False, tries=10000):
+    """n bubbles with amplitude and horizontal radius drawn uniformly (seeded); centred: one
+    bubble at mid-domain, else positions drawn at random so that no two bubbles overlap and
+    none crosses the domain edge."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        amp = float(rng.uniform(*amplitude))
+        rh = float(rng.uniform(*radius))
+        if centred:
+            out.append((amp, rh, 0.5 * lx, 0.5 * ly))
+            continue
+        for _ in range(tries):
+            xc, yc = float(rng.uniform(rh, lx - rh)), float(rng.uniform(rh, ly - rh))
+            if all((xc - b[2]) ** 2 + (yc - b[3]) ** 2 > (rh + b[1]) ** 2 for b in out):
+                break
+        else:
+            raise ValueError("no room for %d non-overlapping bubbles" % n)
+        out.append((amp, rh, xc, yc))
+    return out
+
