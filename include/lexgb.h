@@ -52,6 +52,8 @@ typedef struct lexgb_config {
     double f_cor;            /* Coriolis parameter (namelist_n_constants.py:39) */
     double theta_ref;        /* constant subtracted from theta on the device; 0 = use theta0 at the first level */
     int acoustic_pairs;      /* 0 (default): one acoustic sub-step per launch; 1: two per launch (temporal blocking) */
+    int l2_persist;          /* 0 (default): keep the acoustic sub-steps' per-stage inputs (R_u, R_v, R_w, theta_rho)
+                                in a persisting L2 window; -1: normal caching */
 } lexgb_config;
 
 typedef struct lexgb_ctx lexgb_ctx;

@@ -30,7 +30,7 @@ class Config(ctypes.Structure):
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
                 ("dt", ctypes.c_double), ("n_sound", ctypes.c_int), ("turb_opt", ctypes.c_int),
                 ("cor_opt", ctypes.c_int), ("f_cor", ctypes.c_double), ("theta_ref", ctypes.c_double),
-                ("acoustic_pairs", ctypes.c_int)]
+                ("acoustic_pairs", ctypes.c_int), ("l2_persist", ctypes.c_int)]
 
 
 SIGNATURES = {

@@ -91,6 +91,9 @@ struct lexgb_ctx {
   float* sgs_b[4]{};
   float *sgs_lo = nullptr, *sgs_rin = nullptr, *sgs_rout = nullptr, *sgs_corr = nullptr;
   void *sgs_x = nullptr, *sgs_a0 = nullptr, *sgs_a1 = nullptr;
+  // persisting L2 window over R_u, R_v, R_w, theta_rho for the acoustic sub-steps
+  cudaAccessPolicyWindow l2win{};
+  bool l2on = false;
   // graph of one big step
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -183,7 +186,7 @@ int run_stage(lexgb_ctx* c, int s, const State& xi0, const State& xis, const Sta
   for (int l = 1; l <= launches; ++l) {
     AcousticOut tgt = (l == launches && !(alias && launches == 1)) ? O : ((l & 1) ? X : Y);
     if (l <= nsingle)
-      CK(launch_acoustic(c->d, c->ph, c->cols, in, tgt, dtau, c->stream, l & 1));
+      CK(launch_acoustic(c->d, c->ph, c->cols, in, tgt, dtau, c->stream, l & 1, c->l2on ? &c->l2win : nullptr));
     else
       CK(launch_acoustic_pair(c->d, c->ph, c->cols, in, tgt, dtau, c->stream));
     in.u = tgt.u;
@@ -309,6 +312,37 @@ int build_table(lexgb_ctx* c) {
 
 extern "C" {
 
+// The acoustic sub-steps of a stage all read R_u, R_v, R_w and theta_rho (four adjacent arena
+// fields): a persisting L2 window over them (up to the device's set-aside maximum) keeps them
+// on chip across the 16 or 32 sub-steps, so only the moving state streams through HBM.  The
+// set-aside is a limit of this process's context; failures leave normal caching.
+static void setup_l2_window(lexgb_ctx* c) {
+  int dev = 0, max_persist = 0, max_window = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev) != cudaSuccess ||
+      max_persist <= 0 || max_window <= 0) {
+    cudaGetLastError();
+    return;
+  }
+  size_t bytes = 4 * c->fstride * sizeof(float);
+  if (bytes > (size_t)max_window) bytes = (size_t)max_window;
+  size_t setaside = bytes < (size_t)max_persist ? bytes : (size_t)max_persist;
+  size_t cur = 0;
+  if (cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize) != cudaSuccess) cur = 0;
+  if (cur < setaside && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, setaside) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  if (cur > setaside) setaside = cur;
+  c->l2win.base_ptr = c->Ru;
+  c->l2win.num_bytes = bytes;
+  c->l2win.hitRatio = setaside >= bytes ? 1.0f : (float)setaside / (float)bytes;
+  c->l2win.hitProp = cudaAccessPropertyPersisting;
+  c->l2win.missProp = cudaAccessPropertyStreaming;
+  c->l2on = true;
+}
+
 int lexgb_default_config(lexgb_config* cfg) {
   if (!cfg) return fail(LEXGB_ERR_ARG, "null config");
   memset(cfg, 0, sizeof(*cfg));
@@ -401,6 +435,7 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("counter: ") + cudaGetErrorString(e));
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
+  if (cfg->l2_persist == 0) setup_l2_window(c);
   *out = c;
   return LEXGB_OK;
 }
@@ -409,6 +444,7 @@ int lexgb_destroy(lexgb_ctx* c) {
   if (!c) return LEXGB_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
   drop_graph(c);
+  if (c->l2on) cudaCtxResetPersistingL2Cache();  // return the persisting lines to normal use
   cudaFree(c->arena);
   cudaFree(c->rec_arena);
   cudaFree(c->adj_arena);

@@ -746,7 +746,7 @@ __global__ void k_diag_advpi(Dims d, Phys ph, Cols c, const float* __restrict__ 
 }  // namespace
 
 cudaError_t launch_acoustic(const Dims& d, const Phys& ph, const Cols& c, AcousticIn in, AcousticOut out, float dtau,
-                            cudaStream_t st, int rev) {
+                            cudaStream_t st, int rev, const cudaAccessPolicyWindow* win) {
   constexpr int VW = ACOUSTIC_VEC;
 #if ACOUSTIC_ZMARCH > 0
   if (d.nx % VW == 0) {
@@ -761,6 +761,18 @@ cudaError_t launch_acoustic(const Dims& d, const Phys& ph, const Cols& c, Acoust
     const int nq = d.nx / VW;
     dim3 b(VW == 4 ? 16 : 32, VW == 4 ? 16 : 8, 1);
     dim3 g((nq + b.x - 1) / b.x, (d.ny + b.y - 1) / b.y, d.nz);
+    if (win) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = g;
+      cfg.blockDim = b;
+      cfg.stream = st;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeAccessPolicyWindow;
+      at[0].val.accessPolicyWindow = *win;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      return cudaLaunchKernelEx(&cfg, k_acoustic_vec<VW>, d, ph, c, in, out, dtau, rev);
+    }
     k_acoustic_vec<VW><<<g, b, 0, st>>>(d, ph, c, in, out, dtau, rev);
     return cudaGetLastError();
   }

@@ -283,8 +283,9 @@ struct AcousticIn {
   const float *ps;                  // pi' of the stage state (pip_star)
 };
 struct AcousticOut { float *u, *v, *w, *p; };
+// rev: walk the grid in reversed block order; win: an L2 access-policy window for the launch
 cudaError_t launch_acoustic(const Dims&, const Phys&, const Cols&, AcousticIn in, AcousticOut out, float dtau,
-                            cudaStream_t, int rev = 0);
+                            cudaStream_t, int rev = 0, const cudaAccessPolicyWindow* win = nullptr);
 // two sub-steps in one launch (temporal blocking); in and out must not alias
 cudaError_t launch_acoustic_pair(const Dims&, const Phys&, const Cols&, AcousticIn in, AcousticOut out, float dtau,
                                  cudaStream_t);

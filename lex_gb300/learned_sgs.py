@@ -209,10 +209,16 @@ def step_cost(S, state, net=None, scale=None, n=200):
 
 
 def _select(S, net, series, val, scale, iters, chunk, lr, sprints, log, tag):
-    """Training through the solver in chunks; keeps the weights with the best validation score."""
+    """Training through the solver in chunks, scored on the validation case after each chunk.
+    Candidates: no correction (Smagorinsky alone, the fallback), the starting weights and every
+    chunk; the network is left with the best weights, and `use` is False when no correction
+    scored best."""
     base = float(np.mean(theta_error(S, val)))
-    best = (float(np.mean(theta_error(S, val, net, scale))), net.state_dict(), 0)
-    curve = [{"iters": 0, "val_theta_err": best[0]}]
+    best = (base, None, -1)
+    v0 = float(np.mean(theta_error(S, val, net, scale)))
+    if v0 < best[0]:
+        best = (v0, net.state_dict(), 0)
+    curve = [{"iters": 0, "val_theta_err": v0}]
     for c in range(max(1, iters // chunk)):
         hist = train(S, net, series, scale, iters=chunk, lr=lr, sprints=sprints, seed=1000 + c)
         v = float(np.mean(theta_error(S, val, net, scale)))
@@ -220,11 +226,12 @@ def _select(S, net, series, val, scale, iters, chunk, lr, sprints, log, tag):
         if log:
             log("%s iters %d  mean loss %.4g  validation theta' error %.4f (Smagorinsky %.4f)"
                 % (tag, (c + 1) * chunk, np.mean(hist), v, base))
-        if v < best[0]:
+        if v == v and v < best[0]:
             best = (v, net.state_dict(), (c + 1) * chunk)
-    net.load_state_dict(best[1])
+    if best[1] is not None:
+        net.load_state_dict(best[1])
     return {"val_theta_err_smagorinsky": base, "val_theta_err_learned": best[0], "best_iters": best[2],
-            "curve": curve}
+            "use": best[1] is not None, "curve": curve}
 
 
 def experiment(n_train=8, iters_prior=300, iters=600, chunk=100, lr_prior=1e-3, lr=3e-5, sprints=2, log=print):
@@ -253,10 +260,12 @@ def experiment(n_train=8, iters_prior=300, iters=600, chunk=100, lr_prior=1e-3, 
     scratch_net = sgs_cnn.SGSNet(seed=0)
     sel_scratch = _select(S, scratch_net, series, val, scale, iters, chunk, lr, sprints, log, "from scratch")
     if sel_prior["val_theta_err_learned"] <= sel_scratch["val_theta_err_learned"]:
-        net, branch = prior_net, "a-priori weights"
+        net, sel, branch = prior_net, sel_prior, "a-priori weights"
     else:
-        net, branch = scratch_net, "untrained network"
-    learned = theta_error(S, held, net, scale)
+        net, sel, branch = scratch_net, sel_scratch, "untrained network"
+    if not sel["use"]:
+        branch = "no correction (Smagorinsky scored best on validation)"
+    learned = theta_error(S, held, net, scale) if sel["use"] else list(base)
     cost_plain = step_cost(S, held[0])
     cost_learned = step_cost(S, held[0], net, scale)
     S.close()
@@ -272,9 +281,10 @@ def experiment(n_train=8, iters_prior=300, iters=600, chunk=100, lr_prior=1e-3, 
 def experiment_large(net_state=None, iters=300, chunk=50, lr=3e-5, sprints=2, t_end=1800.0, fine_dt=0.5, log=print):
     """The 128 x 128 x 64 case (76.8 x 76.8 x 19.2 km at 600 x 600 x 300 m, dt 3 s): four
     non-overlapping bubbles with amplitude U(1, 3) K, radius U(1.5, 3) km; 100 m runs (768 x 768 x
-    192, dt `fine_dt`) coarse-grained; the network (from `net_state`, else new) is trained through the solver
-    with `sprints` x 10-step unrolls on one run, selected on a second, evaluated on a third over
-    t_end against Smagorinsky alone; the cost of a corrected step against a plain one."""
+    192, dt `fine_dt`) coarse-grained; the network (from `net_state`, else untrained: last layer
+    zero) is trained through the solver with `sprints` x 10-step unrolls on one run, selected on a
+    second (Smagorinsky alone is a candidate), evaluated on a third over t_end against Smagorinsky
+    alone; the cost of a corrected step against a plain one."""
     t0 = time.time()
     L = (76800.0, 76800.0)
     fine, dims = (768, 768, 192), (128, 128, 64)
@@ -292,7 +302,7 @@ def experiment_large(net_state=None, iters=300, chunk=50, lr=3e-5, sprints=2, t_
         net.load_state_dict(net_state)
     start = theta_error(S, held, net, scale)
     sel = _select(S, net, [train_s], val, scale, iters, chunk, lr, sprints, log, "128x128x64")
-    learned = theta_error(S, held, net, scale)
+    learned = theta_error(S, held, net, scale) if sel["use"] else list(base)
     cost_plain = step_cost(S, held[0])
     cost_learned = step_cost(S, held[0], net, scale)
     S.close()

@@ -35,10 +35,11 @@ class Solver:
     n_sound acoustic sub-steps per big step, turb_opt (0/1), cor_opt (0/1/2), f_cor.
     theta_ref is the constant subtracted from theta on the device (0: theta0 at level 1).
     acoustic_pairs: advance two acoustic sub-steps per kernel launch (temporal blocking).
+    l2_persist: keep the acoustic sub-steps' per-stage inputs in a persisting L2 window.
     """
 
     def __init__(self, nx, ny, nz, dx, dy, dz, dt, n_sound=32, turb_opt=1, cor_opt=0, f_cor=1.0e-4,
-                 theta_ref=0.0, acoustic_pairs=False):
+                 theta_ref=0.0, acoustic_pairs=False, l2_persist=True):
         self.lib = _lib.load()
         cfg = Config()
         check(self.lib.lexgb_default_config(ctypes.byref(cfg)))
@@ -47,6 +48,7 @@ class Solver:
         cfg.n_sound, cfg.turb_opt, cfg.cor_opt = n_sound, turb_opt, cor_opt
         cfg.f_cor, cfg.theta_ref = f_cor, theta_ref
         cfg.acoustic_pairs = 1 if acoustic_pairs else 0
+        cfg.l2_persist = 0 if l2_persist else -1
         self.cfg = cfg
         self.nx, self.ny, self.nz = nx, ny, nz
         self.dt = dt
