@@ -991,6 +991,36 @@ int ensure_adjoint(lexgb_ctx* c, AdjWork& w) {
   return LEXGB_OK;
 }
 
+// A persisting L2 window over [base, base + bytes) when the context uses them (l2_persist):
+// the process's set-aside is raised to cover it, up to the device maximum.
+bool l2_window_for(lexgb_ctx* c, void* base, size_t bytes, cudaAccessPolicyWindow* win) {
+  if (!c->l2on) return false;
+  int dev = 0, max_persist = 0, max_window = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev) != cudaSuccess ||
+      max_persist <= 0 || max_window <= 0) {
+    cudaGetLastError();
+    return false;
+  }
+  if (bytes > (size_t)max_window) bytes = (size_t)max_window;
+  size_t want = bytes < (size_t)max_persist ? bytes : (size_t)max_persist, cur = 0;
+  if (cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize) != cudaSuccess) cur = 0;
+  if (cur < want) {
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    cur = want;
+  }
+  win->base_ptr = base;
+  win->num_bytes = bytes;
+  win->hitRatio = cur >= bytes ? 1.0f : (float)cur / (float)bytes;
+  win->hitProp = cudaAccessPropertyPersisting;
+  win->missProp = cudaAccessPropertyStreaming;
+  return true;
+}
+
 int zero_state(lexgb_ctx* c, const State& s) {
   for (int f = 0; f < NFIELD; ++f) CK(cudaMemsetAsync(field_of(s, f), 0, c->fstride * sizeof(float), c->stream));
   return LEXGB_OK;
@@ -1045,7 +1075,10 @@ int adj_reverse(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages, const fl
   CKS(zero_state(c, w.Xb0));
   if (turb)
     for (int f = 0; f < 5; ++f) CK(cudaMemsetAsync(w.sgsb[f], 0, c->fstride * sizeof(float), c->stream));
-  // ---- reverse
+  // ---- reverse.  The acoustic adjoints read and write the five accumulators (adjacent fields)
+  // in every sub-step: a persisting L2 window keeps them on chip through a stage.
+  cudaAccessPolicyWindow awin{};
+  const bool awin_on = l2_window_for(c, w.Rub, 5 * c->fstride * sizeof(float), &awin);
   for (int s = nstages - 1; s >= 0; --s) {
     const State xs = s == 0 ? A : w.S[s];
     CKS(zero_state(c, w.Xs));
@@ -1059,7 +1092,7 @@ int adj_reverse(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages, const fl
       AcousticVjpArgs a{oldp, w.trho[s], xs.p, w.ac[s][m][0], w.ac[s][m][1], w.ac[s][m][2],
                         adj[0], adj[1], adj[2], adj[3], o[0], o[1], o[2], o[3],
                         w.Rub, w.Rvb, w.Rwb, w.trhob, w.psb};
-      CK(launch_acoustic_vjp(d, c->ph, c->cols, a, (float)p.dtau[s], c->stream));
+      CK(launch_acoustic_vjp(d, c->ph, c->cols, a, (float)p.dtau[s], c->stream, awin_on ? &awin : nullptr));
       for (int f = 0; f < 4; ++f) adj[f] = o[f];
     }
     CK(launch_axpy(w.Xb0.u, adj[0], faces, c->stream));

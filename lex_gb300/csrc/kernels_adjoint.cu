@@ -922,13 +922,25 @@ __global__ void __launch_bounds__(AB) k_smag_state_vjp(Dims d, Phys ph, Cols c, 
 }  // namespace
 
 cudaError_t launch_acoustic_vjp(const Dims& d, const Phys& ph, const Cols& c, const AcousticVjpArgs& a, float dtau,
-                                cudaStream_t st) {
+                                cudaStream_t st, const cudaAccessPolicyWindow* win) {
   constexpr int V = ACOUSTIC_VJP_VEC;
   if (d.nx % V == 0) {
     // small blocks: many registers per thread (a register cap that made the 4-wide kernel spill
     // float4 values faulted with a misaligned address)
     dim3 b(16, 4, 1);
     dim3 g((d.nx / V + 15) / 16, (d.ny + 3) / 4, d.nz);
+    if (win) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = g;
+      cfg.blockDim = b;
+      cfg.stream = st;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeAccessPolicyWindow;
+      at[0].val.accessPolicyWindow = *win;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      return cudaLaunchKernelEx(&cfg, k_acoustic_vjpv<V>, d, ph, c, a, dtau);
+    }
     k_acoustic_vjpv<V><<<g, b, 0, st>>>(d, ph, c, a, dtau);
     return cudaGetLastError();
   }

@@ -55,8 +55,9 @@ struct SmagVjpArgs {
 cudaError_t launch_smag_vjp(const Dims&, const Phys&, const Cols&, State x0, const SmagLin&, const SmagVjpArgs&,
                             cudaStream_t);
 
+// win: an L2 access-policy window for the launch (the accumulators)
 cudaError_t launch_acoustic_vjp(const Dims&, const Phys&, const Cols&, const AcousticVjpArgs&, float dtau,
-                                cudaStream_t);
+                                cudaStream_t, const cudaAccessPolicyWindow* win = nullptr);
 cudaError_t launch_stage_pointwise_vjp(const Dims&, const Phys&, const Cols&, const StageVjpArgs&, cudaStream_t);
 cudaError_t launch_massdiv_vjp(const Dims&, const Phys&, const Cols&, const float* divb, State xsb, cudaStream_t);
 cudaError_t launch_adv_vjp(const Dims&, const Phys&, const Cols&, const AdvVjpArgs&, cudaStream_t);
