@@ -113,8 +113,8 @@ def _advance(phys_state, base_state, model_opt, nsteps, sgs=None):
     return out
 
 
-def _sgs_tensors(dl_params, scaling_params, nx, ny, nz):
-    """The reference's simpleCNN parameters and scaling_params as the library's device tensors.
+def sgs_arrays(dl_params, scaling_params, nx, ny, nz):
+    """The reference's simpleCNN parameters and scaling_params in the library's layout (NumPy).
 
     dl_params: {'Conv_0' .. 'Conv_3': {'kernel': [3, 3, 3, cin, cout] (x, y, z offsets), 'bias':
     [cout]}} (dl_models.py:19-30, flax: cross-correlation, zero padding) -> BF16 [27][cout][cin]
@@ -124,8 +124,8 @@ def _sgs_tensors(dl_params, scaling_params, nx, ny, nz):
     and max - min + 0.01 (1e-5 for qv) over x and y (dl_models.py:128-152); output: the per-cell
     max - min (one_sprint_functions.py:139-143).  Where the reference's ranges live on faces
     (u, v, w), the two faces of a cell are averaged, because the library scales the cell-centred
-    correction before staggering it."""
-    import torch
+    correction before staggering it.  Returns (weights [27][cout][cin] FP32 per layer, biases,
+    {'lo', 'rin': [5][nz], 'rout': [5][nz][ny][nx]})."""
     from . import sgs_cnn
     ws, bs = [], []
     for li, (cin, cout, _) in enumerate(sgs_cnn.LAYERS):
@@ -137,8 +137,8 @@ def _sgs_tensors(dl_params, scaling_params, nx, ny, nz):
         w[:, :k.shape[4], :k.shape[3]] = k.transpose(2, 1, 0, 4, 3).reshape(27, k.shape[4], k.shape[3])
         b = np.zeros(cout, np.float32)
         b[:k.shape[4]] = np.asarray(p["bias"], np.float32)
-        ws.append(torch.tensor(w).to(torch.bfloat16).cuda())
-        bs.append(torch.tensor(b).cuda())
+        ws.append(w)
+        bs.append(b)
     if len(scaling_params) < 10:
         raise ValueError("scaling_params must hold (theta, u, v, w, qv) minima and maxima")
     lo, rin, rout = [], [], []
@@ -159,8 +159,15 @@ def _sgs_tensors(dl_params, scaling_params, nx, ny, nz):
         lo.append(l)
         rin.append(h - l + margin)
         rout.append(r.transpose(2, 1, 0))
-    dev = lambda a: torch.tensor(np.ascontiguousarray(np.stack(a)), dtype=torch.float32).cuda()
-    return ws, bs, {"lo": dev(lo), "rin": dev(rin), "rout": dev(rout)}
+    return ws, bs, {"lo": np.stack(lo), "rin": np.stack(rin), "rout": np.ascontiguousarray(np.stack(rout))}
+
+
+def _sgs_tensors(dl_params, scaling_params, nx, ny, nz):
+    """sgs_arrays on the device: BF16 weights, FP32 biases and ranges."""
+    import torch
+    ws, bs, sc = sgs_arrays(dl_params, scaling_params, nx, ny, nz)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float32).cuda()
+    return ([dev(w).to(torch.bfloat16) for w in ws], [dev(b) for b in bs], {k: dev(v) for k, v in sc.items()})
 
 
 def _attach(solver, sgs):

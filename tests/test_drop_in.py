@@ -135,3 +135,30 @@ def test_sprint_dl_applies_the_correction_inside_the_step(built_lib):
     again, _ = sp.ws_rk3_sprint(x0, base, None, OK)    # the plain sprint detaches the network
     for a, b in zip(again, plain):
         assert np.array_equal(a, b)
+
+
+def test_scaling_params_convert_to_level_ranges():
+    from lex_gb300 import one_sprint_functions as sp
+    nx, ny, nz = 4, 3, 5
+    r = np.random.default_rng(7)
+    shapes = [(nx, ny, nz), (nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1), (nx, ny, nz)]
+    sc = []
+    for shp in shapes:                                   # keepdims shapes of dataset_generation.py:81-90
+        mn = r.normal(size=shp)[None, None]
+        sc += [mn, mn + r.uniform(0.5, 2.0, size=shp)[None, None]]
+    ws, bs, out = sp.sgs_arrays(_flax_params(1), tuple(sc) + (None,) * 4, nx, ny, nz)
+    assert [w.shape for w in ws] == [(27, 32, 16), (27, 32, 32), (27, 32, 32), (27, 8, 32)]
+    assert not ws[0][:, :, 5:].any() and not ws[3][:, 5:, :].any() and not bs[3][5:].any()
+    th_min, th_max = sc[0][0, 0], sc[1][0, 0]
+    assert np.allclose(out["lo"][0], th_min.min(axis=(0, 1)))
+    assert np.allclose(out["rin"][0], th_max.max(axis=(0, 1)) - th_min.min(axis=(0, 1)) + 0.01)
+    assert np.allclose(out["rout"][0], (th_max - th_min).transpose(2, 1, 0))
+    w_min, w_max = sc[6][0, 0], sc[7][0, 0]                # w on faces: the two faces of a cell averaged
+    lo_f = w_min.min(axis=(0, 1))
+    assert np.allclose(out["lo"][3], 0.5 * (lo_f[:-1] + lo_f[1:]))
+    rw = w_max - w_min
+    assert np.allclose(out["rout"][3], (0.5 * (rw[:, :, :-1] + rw[:, :, 1:])).transpose(2, 1, 0))
+    ru = sc[3][0, 0] - sc[2][0, 0]                          # u on x faces
+    assert np.allclose(out["rout"][1], (0.5 * (ru[:-1] + ru[1:])).transpose(2, 1, 0))
+    q_min, q_max = sc[8][0, 0], sc[9][0, 0]
+    assert np.allclose(out["rin"][4], q_max.max(axis=(0, 1)) - q_min.min(axis=(0, 1)) + 1e-5)

@@ -76,3 +76,20 @@ def test_unpack_staggers_the_correction():
     # w: interior face 1 gets half of the bottom cell's correction (range 4); face 0 stays zero
     assert w[1, 0, 0] == 2.0 and float(w.abs().sum()) == 2.0 and float(w[0].abs().sum()) == 0.0
     assert float(v.abs().sum()) == 0.0 and float(p.abs().sum()) == 0.0 and float(q.abs().sum()) == 0.0
+
+
+def test_bubble_generators():
+    import numpy as np
+    from lex_gb300.workload import random_bubbles, warm_bubble, warm_bubbles
+    a, pa = warm_bubble(16, 12, 10, 600.0, 600.0, 300.0, seed=4)
+    b, pb = warm_bubbles(16, 12, 10, 600.0, 600.0, 300.0, [(2.0, 2000.0, 4800.0, 3600.0)], seed=4)
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    four = random_bubbles(3, 4, 76800.0, 76800.0)
+    assert four == random_bubbles(3, 4, 76800.0, 76800.0)          # seeded
+    for i, (amp, rh, xc, yc) in enumerate(four):
+        assert 1.0 <= amp <= 3.0 and 1500.0 <= rh <= 3000.0
+        assert rh <= xc <= 76800.0 - rh and rh <= yc <= 76800.0 - rh
+        for amp2, rh2, xc2, yc2 in four[:i]:
+            assert (xc - xc2) ** 2 + (yc - yc2) ** 2 > (rh + rh2) ** 2
+    one = random_bubbles(5, 1, 19200.0, 19200.0, centred=True)
+    assert one[0][2:] == (9600.0, 9600.0)
