@@ -218,6 +218,9 @@ constexpr int SGS_CIN[4] = {16, 32, 32, 32}, SGS_COUT[4] = {32, 32, 32, 8};
 
 int run_sgs(lexgb_ctx* c) {
   const Dims& d = c->d;
+  // programmatic dependent launches only on a created stream (the step graph is captured on the
+  // context's own stream); on the legacy or per-thread default stream, plain stream order
+  const bool pdl = c->stream != nullptr && c->stream != cudaStreamLegacy && c->stream != cudaStreamPerThread;
   CK(launch_sgs_pack(d.nx, d.ny, d.nz, c->A.T, c->A.u, c->A.v, c->A.w, c->A.q, (float)c->theta_ref, c->sgs_lo,
                      c->sgs_rin, c->sgs_x, c->stream));
   const void* in[4] = {c->sgs_x, c->sgs_a0, c->sgs_a1, c->sgs_a0};
@@ -228,10 +231,10 @@ int run_sgs(lexgb_ctx* c) {
     // lexgb_set_sgs_net, so each layer stages them while the previous kernel finishes
     CK(launch_cnn_conv3d(d.nx, d.ny, d.nz, SGS_CIN[l], SGS_COUT[l], in[l], c->sgs_w[l], c->sgs_b[l], nullptr,
                          last ? nullptr : out[l], last ? c->sgs_corr : nullptr, last ? 0 : 1, last ? 5 : SGS_COUT[l],
-                         c->stream, true));
+                         c->stream, pdl));
   }
   CK(launch_sgs_unpack(d.nx, d.ny, d.nz, c->sgs_corr, c->sgs_rout, c->A.T, c->A.u, c->A.v, c->A.w, c->A.q,
-                       c->stream));
+                       c->stream, pdl));
   return LEXGB_OK;
 }
 

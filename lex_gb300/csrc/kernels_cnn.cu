@@ -438,26 +438,30 @@ __global__ void k_sgs_unpack(int nx, int ny, int nz, const float* __restrict__ c
 }
 }  // namespace
 
-// Persistent-grid size of k_conv3d_smem<CIN, COUT> (resident blocks on the device), set up once:
-// the dynamic shared-memory opt-in and the occupancy query are not stream operations, so they
-// run here (conv_prepare) before any graph capture.
+// Persistent-grid size of k_conv3d_smem<CIN, COUT> (resident blocks on the current device), set
+// up once per device: the dynamic shared-memory opt-in and the occupancy query are not stream
+// operations, so they run here (conv_prepare) before any graph capture.
+constexpr int CONV_MAX_DEVICES = 64;
+
 template <int CIN, int COUT>
 cudaError_t conv_grid(int* cap) {
-  static int grid_cap = 0;
-  if (!grid_cap) {
+  static int grid_cap[CONV_MAX_DEVICES] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= CONV_MAX_DEVICES) return cudaErrorInvalidDevice;
+  if (!grid_cap[dev]) {
     using L = ConvSmem<CIN, COUT>;
-    cudaError_t e =
-        cudaFuncSetAttribute(k_conv3d_smem<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::BYTES);
+    e = cudaFuncSetAttribute(k_conv3d_smem<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::BYTES);
     if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0, per = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    int sms = 0, per = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv3d_smem<CIN, COUT>, L::THREADS, L::BYTES)) !=
         cudaSuccess)
       return e;
-    grid_cap = sms * (per > 0 ? per : 1);
+    grid_cap[dev] = sms * (per > 0 ? per : 1);
   }
-  *cap = grid_cap;
+  *cap = grid_cap[dev];
   return cudaSuccess;
 }
 
@@ -520,7 +524,7 @@ cudaError_t launch_sgs_pack(int nx, int ny, int nz, const float* T, const float*
 }
 
 cudaError_t launch_sgs_unpack(int nx, int ny, int nz, const float* corr, const float* rout, float* T, float* u,
-                              float* v, float* w, float* q, cudaStream_t st) {
+                              float* v, float* w, float* q, cudaStream_t st, bool pdl) {
   const long long n = (long long)nx * ny * nz;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)((n + 255) / 256));
@@ -530,7 +534,7 @@ cudaError_t launch_sgs_unpack(int nx, int ny, int nz, const float* corr, const f
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = pdl ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, k_sgs_unpack, nx, ny, nz, corr, rout, T, u, v, w, q);
 }
 }  // namespace lexgb

@@ -313,7 +313,7 @@ cudaError_t launch_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const v
                               const float* bias, float* pre, void* ybf, float* yf, int gelu, int creal,
                               cudaStream_t st, bool pdl);
 cudaError_t launch_sgs_unpack(int nx, int ny, int nz, const float* corr, const float* rout, float* T, float* u,
-                              float* v, float* w, float* q, cudaStream_t);
+                              float* v, float* w, float* q, cudaStream_t, bool pdl);
 
 // layout conversion between the reference's padded [x][y][z] host layout and the device layout
 // kind: 0 scalar, 1 u, 2 v, 3 w

@@ -61,6 +61,9 @@ def test_fused_correction_matches_torch_path(built_lib):
         lag.set_state(S, x0)
         S.step(1)
         y = lag.get_state(S)
+        lag.set_state(S, x0)
+        S.step(1, graph=False)                     # the same kernels in plain stream order
+        y_eager = lag.get_state(S)
         sgs_cnn.attach(S, None, None)
         lag.set_state(S, x0)
         S.step(1)
@@ -75,6 +78,8 @@ def test_fused_correction_matches_torch_path(built_lib):
     assert torch.equal(y[4], y_plain[4])            # pi' is not corrected
     assert torch.equal(y[3][0], y_plain[3][0]) and torch.equal(y[3][-1], y_plain[3][-1])   # bottom, lid
     for a, b in zip(y_off, y_plain):                 # turning it off restores the plain step
+        assert torch.equal(a, b)
+    for a, b in zip(y_eager, y):                     # graph and plain launches agree bit for bit
         assert torch.equal(a, b)
 
 
