@@ -54,6 +54,7 @@ typedef struct lexgb_config {
     int acoustic_pairs;      /* 0 (default): one acoustic sub-step per launch; 1: two per launch (temporal blocking) */
     int l2_persist;          /* 0 (default): keep the acoustic sub-steps' per-stage inputs (R_u, R_v, R_w, theta_rho)
                                 in a persisting L2 window; -1: normal caching */
+    double cs;               /* Smagorinsky constant; 0 (default): 0.18 (turbulence.py:433) */
 } lexgb_config;
 
 typedef struct lexgb_ctx lexgb_ctx;
@@ -208,6 +209,14 @@ int lexgb_step_vjp(lexgb_ctx *ctx, int nstages, const float *const ybar[6], floa
  * recomputing the step (LEXGB_ERR_STATE if there is no kept step: lexgb_step_vjp and a new base
  * state discard it).  Together they are the non-checkpointed forward + reverse of training. */
 int lexgb_step_keep(lexgb_ctx *ctx);
+/* The Smagorinsky constant Cs (> 0) for the following steps (no counterpart in the reference,
+ * where it is the constant of turbulence.py:433).  lexgb_get_cs_grad: the derivative of the
+ * reverse-mode seeds' inner product with respect to Cs, accumulated over every lexgb_step_vjp /
+ * lexgb_step_vjp_kept call since the last reset (turb_opt 1; FP64 on the device); reset != 0
+ * zeroes the accumulator after reading it.  Together with the state adjoints this is the
+ * gradient of jax.vjp of the sprint with respect to (state, Cs). */
+int lexgb_set_cs(lexgb_ctx *ctx, double cs);
+int lexgb_get_cs_grad(lexgb_ctx *ctx, double *grad, int reset);
 int lexgb_step_vjp_kept(lexgb_ctx *ctx, const float *const ybar[6], float *xbar[6], int on_device);
 
 /* ---- learned SGS correction: the 3-D CNN of dl_models.py:19-30 (simpleCNN) ----

@@ -30,7 +30,7 @@ class Config(ctypes.Structure):
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
                 ("dt", ctypes.c_double), ("n_sound", ctypes.c_int), ("turb_opt", ctypes.c_int),
                 ("cor_opt", ctypes.c_int), ("f_cor", ctypes.c_double), ("theta_ref", ctypes.c_double),
-                ("acoustic_pairs", ctypes.c_int), ("l2_persist", ctypes.c_int)]
+                ("acoustic_pairs", ctypes.c_int), ("l2_persist", ctypes.c_int), ("cs", ctypes.c_double)]
 
 
 SIGNATURES = {
@@ -65,6 +65,8 @@ SIGNATURES = {
     "lexgb_cnn_adam": (_I, [ctypes.c_longlong, _P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                             ctypes.c_float, _I, _P]),
     "lexgb_set_sgs_net": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), _P, _P, _P, _I]),
+    "lexgb_set_cs": (_I, [_P, ctypes.c_double]),
+    "lexgb_get_cs_grad": (_I, [_P, ctypes.POINTER(ctypes.c_double), _I]),
     "lexgb_last_error": (_I, [ctypes.c_char_p, ctypes.c_size_t]),
 }
 

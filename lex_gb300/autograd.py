@@ -8,7 +8,9 @@ steps keeps N states alive, not N times the ~50 intermediate fields of a step.  
 ``jax.vjp`` / ``jax.grad`` through ``ws_rk3_sprint_dl_train`` (one_sprint_functions.py:33-96,
 lex_dl_train.py:114).  The forward keeps the intermediates of the step it ran last
 (``lexgb_step_keep``), so the backward of the most recent step reuses them instead of
-recomputing (``lexgb_step_vjp_kept``); earlier steps of a rollout are recomputed.
+recomputing (``lexgb_step_vjp_kept``); earlier steps of a rollout are recomputed.  The
+Smagorinsky constant can be an input too (``step(solver, state, cs=tensor)``): its gradient is
+the library's FP64 accumulation of the derivative through every step's eddy viscosity.
 
 State layout: a tuple of six float32 CUDA tensors in the device layout, x fastest -
 theta [K], u, v, pi', qv of shape (nz, ny, nx) and w of shape (nz+1, ny, nx) (u on west faces,
@@ -66,7 +68,11 @@ def get_state(solver):
 
 class _Step(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, solver, *state):
+    def forward(ctx, solver, cs, *state):
+        if cs is not None and float(cs) != solver.cs:
+            _bind_stream(solver)
+            solver.set_cs(float(cs))
+        ctx.with_cs = cs is not None
         set_state(solver, state)
         _bind_stream(solver)
         _lib.check(solver.lib.lexgb_step_keep(solver.handle))
@@ -84,24 +90,28 @@ class _Step(torch.autograd.Function):
                    for g, s in zip(grads, _shapes(solver)))
         gx = tuple(torch.empty(s, dtype=torch.float32, device="cuda") for s in _shapes(solver))
         _bind_stream(solver)
+        if ctx.with_cs:
+            solver.cs_grad(reset=True)                          # start this step's accumulation at zero
         if getattr(solver, "_kept_token", None) == ctx.token:   # this step's intermediates are still kept
             _lib.check(solver.lib.lexgb_step_vjp_kept(solver.handle, _ptrs(gy), _ptrs(gx), 1))
         else:                                                   # recompute from the saved input
             set_state(solver, ctx.saved_tensors)
             _lib.check(solver.lib.lexgb_step_vjp(solver.handle, 3, _ptrs(gy), _ptrs(gx), 1))
         solver._kept_token = None
-        return (None,) + gx
+        gcs = torch.tensor(solver.cs_grad(reset=True), dtype=torch.float64, device="cuda") if ctx.with_cs else None
+        return (None, gcs) + gx
 
 
-def step(solver, state):
-    """One differentiable big step: state -> next state (tuples of six CUDA tensors)."""
+def step(solver, state, cs=None):
+    """One differentiable big step: state -> next state (tuples of six CUDA tensors); cs: an
+    optional scalar tensor, the Smagorinsky constant of the step, differentiable."""
     if not isinstance(solver, Solver):
         raise TypeError("solver must be a lex_gb300.solver.Solver")
-    return _Step.apply(solver, *state)
+    return _Step.apply(solver, cs, *state)
 
 
-def rollout(solver, state, nsteps):
+def rollout(solver, state, nsteps, cs=None):
     """nsteps differentiable big steps (the sprint of one_sprint_functions.py:109-115)."""
     for _ in range(int(nsteps)):
-        state = step(solver, state)
+        state = step(solver, state, cs)
     return state

@@ -91,6 +91,9 @@ struct lexgb_ctx {
   float* sgs_b[4]{};
   float *sgs_lo = nullptr, *sgs_rin = nullptr, *sgs_rout = nullptr, *sgs_corr = nullptr;
   void *sgs_x = nullptr, *sgs_a0 = nullptr, *sgs_a1 = nullptr;
+  // Smagorinsky constant and the FP64 accumulator of d(seed . output)/dCs
+  double cs = kCs;
+  double* cs_bar = nullptr;
   // persisting L2 window over R_u, R_v, R_w, theta_rho for the acoustic sub-steps
   cudaAccessPolicyWindow l2win{};
   bool l2on = false;
@@ -376,6 +379,7 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
   if (cfg->turb_opt != 0 && cfg->turb_opt != 1)
     return fail(LEXGB_ERR_ARG, "turb_opt must be 0 or 1 (the anisotropic turb_opt=2 is not provided)");
   if (cfg->cor_opt < 0 || cfg->cor_opt > 2) return fail(LEXGB_ERR_ARG, "cor_opt must be 0, 1 or 2");
+  if (!(cfg->cs >= 0.0)) return fail(LEXGB_ERR_ARG, "cs must be >= 0 (0: the default 0.18)");
   if (cfg->acoustic_pairs != 0 && cfg->acoustic_pairs != 1) return fail(LEXGB_ERR_ARG, "acoustic_pairs must be 0 or 1");
   lexgb_ctx* c = new lexgb_ctx();
   c->cfg = *cfg;
@@ -386,7 +390,8 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
   c->ph.rdx = (float)(1.0 / cfg->dx);
   c->ph.rdy = (float)(1.0 / cfg->dy);
   c->ph.rdz = (float)(1.0 / cfg->dz);
-  const double l = kCs * cbrt(cfg->dx * cfg->dy * cfg->dz);
+  c->cs = cfg->cs > 0.0 ? cfg->cs : kCs;
+  const double l = c->cs * cbrt(cfg->dx * cfg->dy * cfg->dz);
   c->ph.smag_l2 = (float)(l * l);
   c->ph.cor_opt = cfg->cor_opt;
   c->ph.f_cor = (float)cfg->f_cor;
@@ -436,6 +441,10 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("budget: ") + cudaGetErrorString(e));
   e = cudaMalloc(&c->count, sizeof(unsigned long long));
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("counter: ") + cudaGetErrorString(e));
+  e = cudaMalloc(&c->cs_bar, sizeof(double));
+  if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("Cs gradient: ") + cudaGetErrorString(e));
+  e = cudaMemsetAsync(c->cs_bar, 0, sizeof(double), c->stream);
+  if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("Cs gradient: ") + cudaGetErrorString(e));
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
   if (cfg->l2_persist == 0) setup_l2_window(c);
@@ -458,6 +467,7 @@ int lexgb_destroy(lexgb_ctx* c) {
   cudaFree(c->partial);
   cudaFree(c->budget);
   cudaFree(c->count);
+  cudaFree(c->cs_bar);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return LEXGB_OK;
@@ -642,6 +652,26 @@ int lexgb_set_sgs_net(lexgb_ctx* c, const void* const w[4], const float* const b
     drop_graph(c);
   }
   c->sgs_on = true;
+  return LEXGB_OK;
+}
+
+int lexgb_set_cs(lexgb_ctx* c, double cs) {
+  if (!c) return fail(LEXGB_ERR_ARG, "null context");
+  if (!(cs > 0.0)) return fail(LEXGB_ERR_ARG, "cs must be positive");
+  CK(cudaStreamSynchronize(c->stream));
+  const double l = cs * cbrt(c->cfg.dx * c->cfg.dy * c->cfg.dz);
+  c->cs = cs;
+  c->ph.smag_l2 = (float)(l * l);
+  c->adj_kept = false;  // a kept step used the previous constant
+  drop_graph(c);
+  return LEXGB_OK;
+}
+
+int lexgb_get_cs_grad(lexgb_ctx* c, double* grad, int reset) {
+  if (!c || !grad) return fail(LEXGB_ERR_ARG, "null argument");
+  CK(cudaMemcpyAsync(grad, c->cs_bar, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (reset) CK(cudaMemsetAsync(c->cs_bar, 0, sizeof(double), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   return LEXGB_OK;
 }
 
@@ -946,7 +976,7 @@ struct AdjWork {
   SmagVjpArgs sv;
 };
 
-int adj_fields(const StagePlan& p) { return 6 + 15 + 4 * (p.n[0] + p.n[1] + p.n[2]) + 18 + 8 + 5 + 6 + 34 + 5 + 22 + 6; }
+int adj_fields(const StagePlan& p) { return 6 + 15 + 4 * (p.n[0] + p.n[1] + p.n[2]) + 18 + 8 + 5 + 6 + 34 + 5 + 22 + 6 + 1; }
 
 int ensure_adjoint(lexgb_ctx* c, AdjWork& w) {
   const StagePlan p = plan_of(c->cfg);
@@ -989,6 +1019,7 @@ int ensure_adjoint(lexgb_ctx* c, AdjWork& w) {
   w.sv.khb = take();
   for (int f = 0; f < 6; ++f) w.sv.sb[f] = take();
   w.sv.n2b = take();
+  w.sv.kmkb = take();
   w.sv.gu = w.sgsb[0]; w.sv.gv = w.sgsb[1]; w.sv.gw = w.sgsb[2]; w.sv.gT = w.sgsb[3]; w.sv.gq = w.sgsb[4];
   if ((size_t)(q - c->adj_arena) > nf * c->fstride) return fail(LEXGB_ERR_STATE, "adjoint workspace layout");
   return LEXGB_OK;
@@ -1139,6 +1170,8 @@ int adj_reverse(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages, const fl
   if (turb) {
     w.sv.x0b = w.Xb0;
     CK(launch_smag_vjp(d, c->ph, c->cols, A, w.sl, w.sv, c->stream));
+    // dK_m/dCs = 2 K_m / Cs: the Cs derivative of this step
+    CK(launch_sum_scaled(d.cells(), w.sv.kmkb, 2.0 / c->cs, c->cs_bar, c->stream));
   }
   for (int f = 0; f < 6; ++f) {
     const size_t n = (f == 3 ? faces : cells) * sizeof(float);

@@ -823,6 +823,7 @@ __global__ void __launch_bounds__(AB) k_smag_s_vjp(Dims d, Cols c, SmagLin l, Sm
     tb[q] = LD(a.tb[q], id);
     kmb += -2.f * s[q] * tb[q];
   }
+  if (a.kmkb) a.kmkb[id] = kmb * km;
   const float S2b = kmb * LD(l.kS, id);
   for (int q = 0; q < 6; ++q) a.sb[q][id] = -2.f * km * tb[q] + S2b * (q < 3 ? 4.f : 8.f) * s[q] / (r * r);
   a.n2b[id] = -S2b / (float)kPrandtl;
@@ -960,6 +961,31 @@ cudaError_t launch_massdiv_vjp(const Dims& d, const Phys& ph, const Cols& c, con
                                cudaStream_t st) {
   const unsigned g = (unsigned)((d.faces() + AB - 1) / AB);
   k_massdiv_vjp<<<g, AB, 0, st>>>(d, ph, c, divb, xsb);
+  return cudaGetLastError();
+}
+
+// out += scale * sum(x): per-thread FP64 partial sums, a block reduction, one atomic a block
+__global__ void __launch_bounds__(256) k_sum_scaled(long long n, const float* __restrict__ x, double scale,
+                                                    double* __restrict__ out) {
+  __shared__ double part[8];
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc += (double)x[i];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int wv = 0; wv < 8; ++wv) s += part[wv];
+    atomicAdd(out, scale * s);
+  }
+}
+
+cudaError_t launch_sum_scaled(long long n, const float* x, double scale, double* out, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  long long b = (n + 255) / 256;
+  if (b > 1024) b = 1024;
+  k_sum_scaled<<<(unsigned)b, 256, 0, st>>>(n, x, scale, out);
   return cudaGetLastError();
 }
 

@@ -50,8 +50,11 @@ struct SmagVjpArgs {
   float* khb;                           // adjoint of K_h
   float* sb[6];                         // adjoint of rho S_ij
   float* n2b;                           // adjoint of N^2
+  float* kmkb;                          // K_m times its adjoint (optional: the Cs derivative)
   State x0b;                            // accumulated adjoint of the state
 };
+// out[0] += scale * sum of x[0..n) (FP64 accumulation)
+cudaError_t launch_sum_scaled(long long n, const float* x, double scale, double* out, cudaStream_t);
 cudaError_t launch_smag_vjp(const Dims&, const Phys&, const Cols&, State x0, const SmagLin&, const SmagVjpArgs&,
                             cudaStream_t);
 

@@ -36,10 +36,11 @@ class Solver:
     theta_ref is the constant subtracted from theta on the device (0: theta0 at level 1).
     acoustic_pairs: advance two acoustic sub-steps per kernel launch (temporal blocking).
     l2_persist: keep the acoustic sub-steps' per-stage inputs in a persisting L2 window.
+    cs: the Smagorinsky constant (None: 0.18, turbulence.py:433).
     """
 
     def __init__(self, nx, ny, nz, dx, dy, dz, dt, n_sound=32, turb_opt=1, cor_opt=0, f_cor=1.0e-4,
-                 theta_ref=0.0, acoustic_pairs=False, l2_persist=True):
+                 theta_ref=0.0, acoustic_pairs=False, l2_persist=True, cs=None):
         self.lib = _lib.load()
         cfg = Config()
         check(self.lib.lexgb_default_config(ctypes.byref(cfg)))
@@ -49,6 +50,8 @@ class Solver:
         cfg.f_cor, cfg.theta_ref = f_cor, theta_ref
         cfg.acoustic_pairs = 1 if acoustic_pairs else 0
         cfg.l2_persist = 0 if l2_persist else -1
+        cfg.cs = float(cs) if cs is not None else 0.0
+        self.cs = float(cs) if cs is not None else 0.18
         self.cfg = cfg
         self.nx, self.ny, self.nz = nx, ny, nz
         self.dt = dt
@@ -148,6 +151,17 @@ class Solver:
     def step(self, nsteps=1, graph=True):
         """Advance nsteps RK3 big steps (asynchronous on the context's stream)."""
         check(self.lib.lexgb_step(self.handle, int(nsteps), 1 if graph else 0))
+
+    def set_cs(self, cs):
+        """Smagorinsky constant for the following steps."""
+        check(self.lib.lexgb_set_cs(self.handle, float(cs)))
+        self.cs = float(cs)
+
+    def cs_grad(self, reset=True):
+        """d(seed . output)/dCs accumulated by the reverse-mode calls since the last reset."""
+        g = ctypes.c_double()
+        check(self.lib.lexgb_get_cs_grad(self.handle, ctypes.byref(g), 1 if reset else 0))
+        return g.value
 
     def step_record(self):
         check(self.lib.lexgb_step_record(self.handle))

@@ -135,8 +135,9 @@ class Dycore:
     theta0, qv0, pi0, rho0 (each (nz+2,)); dt, n_sound; dtype FP64 or FP32.
     """
 
-    def __init__(self, grid, base, dt, n_sound=32, dtype=np.float64, turb=True):
+    def __init__(self, grid, base, dt, n_sound=32, dtype=np.float64, turb=True, cs=CS):
         self.g = grid
+        self.cs = cs
         self.nx, self.ny, self.nz = grid.nx, grid.ny, grid.nz
         self.dt = dt
         self.n_sound = n_sound
@@ -359,7 +360,7 @@ class Dycore:
         delta = np.cbrt(self.dx * self.dy * self.dz)
         s2n2 = s2 - n2 / PRANDTL
         s2n2 = np.where(s2n2 > 0.0, s2n2, 0.0)
-        km = (CS * delta) ** 2 * np.sqrt(s2n2)
+        km = (self.cs * delta) ** 2 * np.sqrt(s2n2)
         return km, km / PRANDTL
 
     def smagorinsky(self, theta, u, v, w, qv):

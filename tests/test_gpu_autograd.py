@@ -67,3 +67,44 @@ def test_rollout_gradient_matches_oracle_finite_differences(built_lib):
     rhs = sum(float(np.sum(a * b)) for a, b in zip(grads, v))
     scale = np.sqrt(sum(float(np.sum(a * a)) for a in yb)) * np.sqrt(sum(float(np.sum(a * a)) for a in jv))
     assert abs(lhs - rhs) <= 1e-4 * scale, (lhs, rhs)
+
+
+def test_rollout_gradient_with_respect_to_cs(built_lib):
+    """d<ybar, x_N>/dCs through torch.autograd (the library's accumulation over each step's eddy
+    viscosity) against a central difference of the FP64 oracle in Cs, eps = 1e-3."""
+    torch = pytest.importorskip("torch")
+    from oracle.ic import Grid
+    from oracle.dycore import Dycore
+    from lex_gb300.solver import Solver
+    from lex_gb300 import autograd as lag
+    g = load_golden("ops_random.npz")
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    base = dict(theta0=g["col_theta0"], qv0=g["col_qv0"], pi0=g["col_pi0"], rho0=g["col_rho0"])
+    grid = Grid(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"]))
+    x0 = tuple(g["in_" + f] for f in FIELDS)
+    cs0 = 0.18
+
+    def forward(cs):
+        D = Dycore(grid, base, float(g["dt"]), int(g["n_sound"]), turb=True, cs=cs)
+        x = x0
+        for _ in range(NSTEPS):
+            x = D.step(x)[0]
+        return _interior(x, nx, ny)
+
+    rng = np.random.default_rng(11)
+    yb = _direction(rng, nx, ny, nz)
+    with Solver(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"]), float(g["dt"]), int(g["n_sound"]),
+                turb_opt=1) as S:
+        S.set_base_columns(g["col_theta0"], g["col_qv0"], g["col_pi0"], g["col_rho0"])
+        state = tuple(_to_dev(a) for a in _interior(x0, nx, ny))
+        cs = torch.tensor(cs0, dtype=torch.float64, device="cuda", requires_grad=True)
+        out = lag.rollout(S, state, NSTEPS, cs=cs)
+        loss = sum((o * _to_dev(y)).sum() for o, y in zip(out, yb))
+        loss.backward()
+        got = float(cs.grad)
+    eps = 1e-3
+    jv = [(a - b) / (2 * eps) for a, b in zip(forward(cs0 + eps), forward(cs0 - eps))]
+    lhs = sum(float(np.sum(a * b)) for a, b in zip(yb, jv))
+    scale = np.sqrt(sum(float(np.sum(a * a)) for a in yb)) * np.sqrt(sum(float(np.sum(a * a)) for a in jv))
+    assert abs(lhs) > 1e-3 * scale                     # Cs matters in this case
+    assert abs(lhs - got) <= 1e-4 * scale, (lhs, got, scale)
