@@ -3,6 +3,7 @@
 // replay of a big step, host transfers, operator diagnostics and FP64 budgets.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -12,6 +13,14 @@
 
 #include "../../include/lexgb.h"
 #include "lexgb_adjoint.cuh"
+
+namespace {
+// NVTX range over an ABI call (no cost without a profiler attached)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+}  // namespace
 
 using namespace lexgb;
 
@@ -512,6 +521,7 @@ int lexgb_integrate_base_state(lexgb_ctx* c, const double* theta0, const double*
 }
 
 int lexgb_upload_state(lexgb_ctx* c, const void* const fields[6], int dtype) {
+  NvtxRange nvtx_range("lexgb_upload_state");
   if (!c || !fields) return fail(LEXGB_ERR_ARG, "null argument");
   if (dtype != LEXGB_F32 && dtype != LEXGB_F64) return fail(LEXGB_ERR_ARG, "dtype must be LEXGB_F32 or LEXGB_F64");
   if (!c->base_set) return fail(LEXGB_ERR_STATE, "set the base state before uploading (theta_ref comes from it)");
@@ -535,6 +545,7 @@ int lexgb_upload_state(lexgb_ctx* c, const void* const fields[6], int dtype) {
 }
 
 int lexgb_download_state(lexgb_ctx* c, void* const fields[6], int dtype) {
+  NvtxRange nvtx_range("lexgb_download_state");
   CKS(check_ready(c));
   if (!fields) return fail(LEXGB_ERR_ARG, "null argument");
   if (dtype != LEXGB_F32 && dtype != LEXGB_F64) return fail(LEXGB_ERR_ARG, "dtype must be LEXGB_F32 or LEXGB_F64");
@@ -554,6 +565,7 @@ int lexgb_download_state(lexgb_ctx* c, void* const fields[6], int dtype) {
 }
 
 int lexgb_step(lexgb_ctx* c, int nsteps, int use_graph) {
+  NvtxRange nvtx_range("lexgb_step");
   CKS(check_ready(c));
   if (nsteps < 0) return fail(LEXGB_ERR_ARG, "nsteps must be >= 0");
   c->recorded = false;
@@ -1192,6 +1204,7 @@ int check_vjp_args(const float* const ybar[6], float* xbar[6]) {
 }  // namespace
 
 int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float* xbar[6], int on_device) {
+  NvtxRange nvtx_range("lexgb_step_vjp");
   CKS(check_ready(c));
   if (nstages < 1 || nstages > 3) return fail(LEXGB_ERR_ARG, "need 1..3 stages");
   CKS(check_vjp_args(ybar, xbar));
@@ -1203,6 +1216,7 @@ int lexgb_step_vjp(lexgb_ctx* c, int nstages, const float* const ybar[6], float*
 }
 
 int lexgb_step_keep(lexgb_ctx* c) {
+  NvtxRange nvtx_range("lexgb_step_keep");
   CKS(check_ready(c));
   AdjWork w;
   CKS(ensure_adjoint(c, w));
@@ -1218,6 +1232,7 @@ int lexgb_step_keep(lexgb_ctx* c) {
 }
 
 int lexgb_step_vjp_kept(lexgb_ctx* c, const float* const ybar[6], float* xbar[6], int on_device) {
+  NvtxRange nvtx_range("lexgb_step_vjp_kept");
   CKS(check_ready(c));
   CKS(check_vjp_args(ybar, xbar));
   if (!c->adj_kept) return fail(LEXGB_ERR_STATE, "no kept step: call lexgb_step_keep first");

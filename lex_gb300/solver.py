@@ -92,6 +92,7 @@ class Solver:
     def set_base_columns(self, theta0, qv0, pi0, rho0):
         cols = [self._col(c) for c in (theta0, qv0, pi0, rho0)]
         check(self.lib.lexgb_set_base_columns(self.handle, *[_dptr(c) for c in cols]))
+        self._base = cols
 
     def set_base_state(self, base_state):
         """From the reference's base_state tuple (rho0_theta0, rho0, theta0, pi0, qv0, surface_t)."""
@@ -111,6 +112,7 @@ class Solver:
         pi0 = np.empty(self.nz + 2)
         rho0 = np.empty(self.nz + 2)
         check(self.lib.lexgb_integrate_base_state(self.handle, _dptr(t), _dptr(q), _dptr(pi0), _dptr(rho0)))
+        self._base = [t, q, pi0.copy(), rho0.copy()]
         return pi0, rho0
 
     # -------------------------------------------------------------------------------- state transfer
@@ -217,6 +219,43 @@ class Solver:
         n = ctypes.c_longlong()
         check(self.lib.lexgb_check_finite(self.handle, ctypes.byref(n)))
         return n.value
+
+    def check_finite(self):
+        """Raise FloatingPointError if the state holds a NaN or an infinity (one device count)."""
+        n = self.count_nonfinite()
+        if n:
+            raise FloatingPointError("%d non-finite values in the solver state" % n)
+
+    # -------------------------------------------------------------------------------- checkpoints
+    _CFG = ("nx", "ny", "nz", "dx", "dy", "dz", "dt", "n_sound", "turb_opt", "cor_opt", "f_cor", "theta_ref",
+            "acoustic_pairs", "l2_persist")
+
+    def save(self, path):
+        """Checkpoint to an .npz archive: the configuration, the Smagorinsky constant, the base
+        columns and the state (padded reference layout, FP64: the device's FP32 values and the
+        theta offset are exact in it, so a restored solver continues bit for bit)."""
+        if getattr(self, "_base", None) is None:
+            raise RuntimeError("no base state has been set")
+        out = {"cfg_" + k: np.asarray(getattr(self.cfg, k)) for k in self._CFG}
+        out["cfg_cs"] = np.asarray(self.cs)
+        for name, c in zip(("theta0", "qv0", "pi0", "rho0"), self._base):
+            out["base_" + name] = c
+        for name, a in zip(FIELDS, self.download(np.float64)):
+            out["state_" + name] = a
+        np.savez(path, **out)
+
+    @classmethod
+    def restore(cls, path):
+        """A new solver from a checkpoint written by save()."""
+        with np.load(path) as z:
+            c = {k: z["cfg_" + k].item() for k in cls._CFG}
+            S = cls(int(c["nx"]), int(c["ny"]), int(c["nz"]), c["dx"], c["dy"], c["dz"], c["dt"], int(c["n_sound"]),
+                    turb_opt=int(c["turb_opt"]), cor_opt=int(c["cor_opt"]), f_cor=c["f_cor"],
+                    theta_ref=c["theta_ref"], acoustic_pairs=bool(c["acoustic_pairs"]),
+                    l2_persist=int(c["l2_persist"]) == 0, cs=z["cfg_cs"].item())
+            S.set_base_columns(*[z["base_" + n] for n in ("theta0", "qv0", "pi0", "rho0")])
+            S.upload(tuple(z["state_" + f] for f in FIELDS))
+        return S
 
     def step_kernel_count(self):
         n = ctypes.c_int()
