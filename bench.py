@@ -193,6 +193,24 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(x, dist=None):
+    """The largest value of x over the ranks of the process group (x itself without one); the
+    reduction tensor lives where the backend wants it (CUDA for NCCL, host memory for gloo)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(ms_local, ws, npts, steps, dist=None):
+    """Whole-job throughput of ws independent replicas, each timing `steps` steps of `npts`
+    points in ms_local: the job takes as long as its slowest replica -> (ms, points*steps/s)."""
+    ms = max_over_ranks(ms_local, dist)
+    return ms, ws * npts * steps / (ms * 1e-3)
+
+
 def run_lexgb(args):
     import torch
     ws, rank, local = dist_env()
@@ -216,13 +234,6 @@ def run_lexgb(args):
         if dist is not None:
             dist.barrier()
 
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
     # ---- device-resident throughput (value)
     S.step(max(3, args.warmup), graph=True)
     S.synchronize()
@@ -241,9 +252,8 @@ def run_lexgb(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     barrier()
-    ms = max_over_ranks(e0.elapsed_time(e1))
+    ms, value = replica_throughput(e0.elapsed_time(e1), ws, npts, args.steps, dist)
     ms_per_step = ms / args.steps
-    value = ws * npts * args.steps / (ms * 1e-3)
     n_bad = S.count_nonfinite()
     if args.profile:   # warm-up + timed steps only (for profiler captures)
         if rank == 0:
@@ -275,7 +285,7 @@ def run_lexgb(args):
         S.step(1, graph=True)
         S.download_ptrs(ptr_out, False)
     torch.cuda.synchronize()
-    el = max_over_ranks(time.perf_counter() - t0)
+    el = max_over_ranks(time.perf_counter() - t0, dist)
     e2e = ws * npts * e2e_steps / el
 
     # ---- dominant kernel: one acoustic sub-step, timed alone with CUDA events
