@@ -15,6 +15,13 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built liblexgb.so")
 
 
+def report_path(name):
+    """Where the GPU tests write their JSON reports: $LEXGB_REPORT_DIR, else reports/ in the repo."""
+    d = os.environ.get("LEXGB_REPORT_DIR") or os.path.join(ROOT, "reports")
+    os.makedirs(d, exist_ok=True)
+    return os.path.join(d, name)
+
+
 def load_golden(name):
     with np.load(os.path.join(GOLDEN, name)) as z:
         return {k: z[k] for k in z.files}

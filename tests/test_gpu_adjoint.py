@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import load_golden, ROOT
+from conftest import load_golden, report_path, ROOT
 from test_gpu_parity import FIELDS
 
 pytestmark = pytest.mark.gpu
@@ -24,8 +24,7 @@ REPORT = {}
 @pytest.fixture(scope="module", autouse=True)
 def report():
     yield
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    with open(os.path.join(ROOT, "gpurun_out", "adjoint_report.json"), "w") as f:
+    with open(report_path("adjoint_report.json"), "w") as f:
         json.dump(REPORT, f, indent=1, sort_keys=True)
 
 

@@ -13,7 +13,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import rel_l2, ROOT
+from conftest import rel_l2, report_path, ROOT
 
 FIELDS = ("theta", "u", "v", "w", "pip", "qv")
 REPORT = {}
@@ -50,8 +50,7 @@ def inner_u(a):
 @pytest.fixture(scope="module", autouse=True)
 def report():
     yield
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    with open(os.path.join(ROOT, "gpurun_out", "parity_report.json"), "w") as f:
+    with open(report_path("parity_report.json"), "w") as f:
         json.dump(REPORT, f, indent=1, sort_keys=True)
 
 
