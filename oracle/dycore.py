@@ -1,9 +1,9 @@
 """Oracle: a NumPy restatement of LEX's fully compressible dynamical-core step (solver_opt=2).
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
-``cpu_baseline`` leg of ``bench.py`` may import this package; the product path
-never does.  It is the checker for the CUDA kernels, pinned in turn against
-golden vectors produced by the reference's own source (tests/golden/).
+``cpu_baseline`` and ``--impl reference`` legs of ``bench.py`` may import this package; the
+product path never does.  The CUDA kernels are tested against it, and it is pinned in turn
+against golden vectors produced by the reference's own source (tests/golden/).
 
 Everything works on the reference's padded ``[x][y][z]`` arrays (see oracle/ic.py)
 in the dtype of the inputs (FP64 for the oracle proper; FP32 reproduces what an

@@ -1,8 +1,8 @@
 """Oracle: grids, base state and warm-bubble initial state in the reference's padded layout.
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
-``cpu_baseline`` leg of ``bench.py`` may import this package; the product path
-never does.
+``cpu_baseline`` and ``--impl reference`` legs of ``bench.py`` may import this package; the
+product path never does.
 
 Layout follows LEX exactly: C-order ``[x][y][z]`` arrays with ``ngx=ngy=3``
 lateral ghost cells and ``ngz=1`` ghost level, scalars ``(nx+6, ny+6, nz+2)``,
