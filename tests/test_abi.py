@@ -78,3 +78,15 @@ def test_new_entry_points_validate_before_touching_the_gpu(lib):
     assert lib.lexgb_cnn_conv3d_dw(16, 4, 4, 48, 32, 32, p, p, p, None, None) == _lib.LEXGB_ERR_ARG
     assert lib.lexgb_cnn_adam(0, p, p, p, p, None, 1e-3, 0.9, 0.999, 1e-8, 1, None) == _lib.LEXGB_ERR_ARG
 
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No CPU fallback: without the built library every entry into the package raises."""
+    from lex_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "liblexgb.so"))
+    with pytest.raises(ImportError):
+        _lib.load()
+    from lex_gb300.solver import Solver
+    with pytest.raises(ImportError):
+        Solver(16, 16, 8, 100.0, 100.0, 100.0, 1.0)
