@@ -12,7 +12,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import load_golden, report_path, ROOT
+from conftest import load_golden, report_path
 from test_gpu_parity import FIELDS
 
 pytestmark = pytest.mark.gpu

@@ -13,7 +13,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import rel_l2, report_path, ROOT
+from conftest import rel_l2, report_path
 
 FIELDS = ("theta", "u", "v", "w", "pip", "qv")
 REPORT = {}

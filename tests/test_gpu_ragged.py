@@ -6,7 +6,6 @@ a tile's halo reach, and nz = 1 and 2 (mod 4), where the last vertical tile hold
 levels and the one-sided top extrapolations reach below the tile.  The oracle (FP64) is the
 reference; it is pinned to the reference's own outputs by tests/test_oracle_golden.py.
 """
-import numpy as np
 import pytest
 
 from conftest import rel_l2

@@ -4,10 +4,9 @@ The golden vectors were produced by running the reference's source under a NumPy
 for jax (tests/golden/make_golden.py); in FP64 the restatement must agree to rounding.
 """
 import numpy as np
-import pytest
 
 from conftest import rel_l2
-from oracle.ic import Grid, WarmBubble, hydrostatic_columns, reference_option1_base_state
+from oracle.ic import Grid, WarmBubble, reference_option1_base_state
 from oracle.dycore import Dycore
 
 FIELDS = ("theta", "u", "v", "w", "pip", "qv")
