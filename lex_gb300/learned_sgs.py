@@ -12,8 +12,8 @@ and, for the a-priori stage, also one coarse step (3 s) later.  Two training sta
   through the solver (lex_dl_train.py:49-131)  from a coarse-grained state, sprints of coarse
              steps with the correction after each step (one_sprint_functions.py:128-163) are
              compared with the coarse-grained truth at the sprints' ends; the loss is the sum over
-             theta, u, v, w, qv of the squared error over each field's range (the reference adds
-             Laplacian and negative-qv terms).  Gradients flow through the solver
+             theta, u, v, w, qv of the squared error over each field's range (its Laplacian and
+             negative-qv terms are options).  Gradients flow through the solver
              (lex_gb300.autograd, step-level checkpointing) and the CNN (lex_gb300.sgs_cnn); the
              weights with the best validation score are kept.
 Evaluation: coarse runs with and without the correction against the coarse-grained fine run,
@@ -87,9 +87,29 @@ def coarse_solver(dims=(32, 32, 32), spacing=(600., 600., 300.), dt=3.0):
     return S
 
 
-def field_scale(snapshots):
-    """Per-level ranges of the training snapshots (the scaling_params of the reference)."""
-    return sgs_cnn.make_scale(snapshots)
+def laplacian(a, spacing):
+    """7-point Laplacian of a cell field [nz][ny][nx]: periodic in x and y, zero gradient through
+    the bottom and the lid (laplace_of_tensor, dataset_generation.py:291-317)."""
+    dx, dy, dz = spacing
+    lx = (torch.roll(a, -1, 2) - 2.0 * a + torch.roll(a, 1, 2)) / (dx * dx)
+    ly = (torch.roll(a, -1, 1) - 2.0 * a + torch.roll(a, 1, 1)) / (dy * dy)
+    z = torch.zeros_like(a[:1])
+    gz = torch.cat([z, (a[1:] - a[:-1]) / dz, z], 0)
+    return lx + ly + (gz[1:] - gz[:-1]) / dz
+
+
+def field_scale(snapshots, spacing=None):
+    """Per-level ranges of the training snapshots (the scaling_params of the reference); with
+    `spacing`, also the ranges of the theta and qv Laplacians (+1e-7, +1e-10) for the Laplacian
+    loss terms."""
+    sc = sgs_cnn.make_scale(snapshots)
+    if spacing is not None:
+        la = []
+        for i, margin in ((0, 1.0e-7), (5, 1.0e-10)):
+            vals = [laplacian(s[i], spacing) for s in snapshots]
+            la.append(float(max(float(v.max()) for v in vals) - min(float(v.min()) for v in vals)) + margin)
+        sc["la"] = la
+    return sc
 
 
 def sprint(S, state, nsteps, net=None, scale=None, grad=True):
@@ -103,18 +123,27 @@ def sprint(S, state, nsteps, net=None, scale=None, grad=True):
     return state
 
 
-def loss_fn(state, truth, scale):
+def loss_fn(state, truth, scale, spacing=None, laplacian_terms=False, neg_qv=False):
     """Sum over theta, u, v, w, qv of the squared error, each field divided by its largest
-    per-level input range (the normalised L2 loss of lex_dl_train.py:49-99 without its Laplacian
-    and negative-qv terms)."""
+    per-level input range (the normalised L2 loss of lex_dl_train.py:49-99).  Options from the
+    same loss: laplacian_terms adds the squared errors of the theta and qv Laplacians over their
+    ranges (needs `spacing` and a scale from field_scale(..., spacing)); neg_qv adds the
+    negative part of qv over its range (lex_dl_train.py:92-97)."""
     total = 0.0
     for f, i in enumerate((0, 1, 2, 3, 5)):
         r = scale["rin"][f].max()
         total = total + ((state[i] - truth[i]) / r).pow(2).sum()
+    if laplacian_terms:
+        for k, i in enumerate((0, 5)):
+            d = laplacian(state[i], spacing) - laplacian(truth[i], spacing)
+            total = total + (d / scale["la"][k]).pow(2).sum()
+    if neg_qv:
+        total = total + torch.relu(-state[5]).sum() / scale["rin"][4].max()
     return total
 
 
-def train(S, net, series, scale, steps_per_sprint=10, iters=200, lr=1e-4, warmup=50, sprints=1, seed=0, log=None):
+def train(S, net, series, scale, steps_per_sprint=10, iters=200, lr=1e-4, warmup=50, sprints=1, seed=0, log=None,
+          laplacian_terms=False, neg_qv=False):
     """Adam on rollouts drawn from the coarse-grained series (lists of snapshot tuples): from a
     snapshot, `sprints` sprints of `steps_per_sprint` corrected coarse steps, the loss summed over
     the snapshots they end at.  The learning rate rises linearly over the first `warmup` steps."""
@@ -129,7 +158,7 @@ def train(S, net, series, scale, steps_per_sprint=10, iters=200, lr=1e-4, warmup
         loss = 0.0
         for j in range(1, sprints + 1):
             state = sprint(S, state, steps_per_sprint, net, scale)
-            loss = loss + loss_fn(state, s[k + j], scale)
+            loss = loss + loss_fn(state, s[k + j], scale, (S.cfg.dx, S.cfg.dy, S.cfg.dz), laplacian_terms, neg_qv)
         grads = torch.autograd.grad(loss, net.params())
         n = net.step_count + 1
         sgs_cnn.adam_step(net, [g.detach() for g in grads], lr=lr * min(1.0, n / max(1, warmup)))
@@ -208,7 +237,7 @@ def step_cost(S, state, net=None, scale=None, n=200):
     return e0.elapsed_time(e1) / n
 
 
-def _select(S, net, series, val, scale, iters, chunk, lr, sprints, log, tag):
+def _select(S, net, series, val, scale, iters, chunk, lr, sprints, log, tag, loss_opts=None):
     """Training through the solver in chunks, scored on the validation case after each chunk.
     Candidates: no correction (Smagorinsky alone, the fallback), the starting weights and every
     chunk; the network is left with the best weights, and `use` is False when no correction
@@ -220,7 +249,7 @@ def _select(S, net, series, val, scale, iters, chunk, lr, sprints, log, tag):
         best = (v0, net.state_dict(), 0)
     curve = [{"iters": 0, "val_theta_err": v0}]
     for c in range(max(1, iters // chunk)):
-        hist = train(S, net, series, scale, iters=chunk, lr=lr, sprints=sprints, seed=1000 + c)
+        hist = train(S, net, series, scale, iters=chunk, lr=lr, sprints=sprints, seed=1000 + c, **(loss_opts or {}))
         v = float(np.mean(theta_error(S, val, net, scale)))
         curve.append({"iters": (c + 1) * chunk, "loss": float(np.mean(hist)), "val_theta_err": v})
         if log:
@@ -234,7 +263,8 @@ def _select(S, net, series, val, scale, iters, chunk, lr, sprints, log, tag):
             "use": best[1] is not None, "curve": curve}
 
 
-def experiment(n_train=8, iters_prior=300, iters=600, chunk=100, lr_prior=1e-3, lr=3e-5, sprints=2, log=print):
+def experiment(n_train=8, iters_prior=300, iters=600, chunk=100, lr_prior=1e-3, lr=3e-5, sprints=2, log=print,
+               laplacian_terms=False, neg_qv=False):
     """The 32^3 case: 100 m runs of one mid-domain bubble with amplitude U(1, 3) K and horizontal
     radius U(1.5, 3) km (seeded), coarse-grained 6 x 6 x 3.  An a-priori stage on one-step
     residuals, then training through the solver (`sprints` x 10-step unrolls) from the a-priori
@@ -248,7 +278,8 @@ def experiment(n_train=8, iters_prior=300, iters=600, chunk=100, lr_prior=1e-3, 
     series = [r[0] for r in runs]
     val = fine_run(bub(200), 200)
     held = fine_run(bub(300), 300)
-    scale = field_scale([x for s in series for x in s])
+    scale = field_scale([x for s in series for x in s], spacing=(600.0, 600.0, 300.0))
+    opts = {"laplacian_terms": laplacian_terms, "neg_qv": neg_qv}
     S = coarse_solver()
     dims = (S.nx, S.ny, S.nz)
     base = theta_error(S, held)
@@ -256,9 +287,9 @@ def experiment(n_train=8, iters_prior=300, iters=600, chunk=100, lr_prior=1e-3, 
     prior_net = sgs_cnn.SGSNet(seed=0)
     hp = pretrain(prior_net, pairs, scale, dims, iters=iters_prior, lr=lr_prior, log=log)
     prior = theta_error(S, held, prior_net, scale)
-    sel_prior = _select(S, prior_net, series, val, scale, iters, chunk, lr, sprints, log, "from a-priori")
+    sel_prior = _select(S, prior_net, series, val, scale, iters, chunk, lr, sprints, log, "from a-priori", opts)
     scratch_net = sgs_cnn.SGSNet(seed=0)
-    sel_scratch = _select(S, scratch_net, series, val, scale, iters, chunk, lr, sprints, log, "from scratch")
+    sel_scratch = _select(S, scratch_net, series, val, scale, iters, chunk, lr, sprints, log, "from scratch", opts)
     if sel_prior["val_theta_err_learned"] <= sel_scratch["val_theta_err_learned"]:
         net, sel, branch = prior_net, sel_prior, "a-priori weights"
     else:
@@ -278,7 +309,8 @@ def experiment(n_train=8, iters_prior=300, iters=600, chunk=100, lr_prior=1e-3, 
             "cost_ratio": cost_learned / cost_plain, "seconds": time.time() - t0, "net": net, "scale": scale}
 
 
-def experiment_large(net_state=None, iters=300, chunk=50, lr=3e-5, sprints=2, t_end=1800.0, fine_dt=0.5, log=print):
+def experiment_large(net_state=None, iters=300, chunk=50, lr=3e-5, sprints=2, t_end=1800.0, fine_dt=0.5, log=print,
+                     laplacian_terms=False, neg_qv=False):
     """The 128 x 128 x 64 case (76.8 x 76.8 x 19.2 km at 600 x 600 x 300 m, dt 3 s): four
     non-overlapping bubbles with amplitude U(1, 3) K, radius U(1.5, 3) km; 100 m runs (768 x 768 x
     192, dt `fine_dt`) coarse-grained; the network (from `net_state`, else untrained: last layer
@@ -294,14 +326,15 @@ def experiment_large(net_state=None, iters=300, chunk=50, lr=3e-5, sprints=2, t_
     train_s, val, held = run(400), run(450), run(500)
     if log:
         log("fine runs done (%.0f s)" % (time.time() - t0))
-    scale = field_scale(train_s)
+    scale = field_scale(train_s, spacing=(600.0, 600.0, 300.0))
     S = coarse_solver(dims=dims)
     base = theta_error(S, held)
     net = sgs_cnn.SGSNet(seed=0)
     if net_state is not None:
         net.load_state_dict(net_state)
     start = theta_error(S, held, net, scale)
-    sel = _select(S, net, [train_s], val, scale, iters, chunk, lr, sprints, log, "128x128x64")
+    sel = _select(S, net, [train_s], val, scale, iters, chunk, lr, sprints, log, "128x128x64",
+                  {"laplacian_terms": laplacian_terms, "neg_qv": neg_qv})
     learned = theta_error(S, held, net, scale) if sel["use"] else list(base)
     cost_plain = step_cost(S, held[0])
     cost_learned = step_cost(S, held[0], net, scale)
@@ -326,20 +359,24 @@ def main(argv=None):
     ap.add_argument("--iters-large", type=int, default=300)
     ap.add_argument("--lr", type=float, default=3e-5)
     ap.add_argument("--sprints", type=int, default=2)
+    ap.add_argument("--laplacian", action="store_true", help="add the theta / qv Laplacian loss terms")
+    ap.add_argument("--neg-qv", action="store_true", help="add the negative-qv loss term")
     ap.add_argument("--init", default=None, help="start the 128 case from the 32^3 network of a previous --out .pt")
     ap.add_argument("--out", default=None, help="JSON summary (one line per case); weights beside it (.pt)")
     a = ap.parse_args(argv)
     lines, nets = [], {}
     state = torch.load(a.init)["32"]["net"] if a.init else None
     if a.case in ("32", "both"):
-        r = experiment(iters_prior=a.iters_prior, iters=a.iters, lr=a.lr, sprints=a.sprints)
+        r = experiment(iters_prior=a.iters_prior, iters=a.iters, lr=a.lr, sprints=a.sprints,
+                       laplacian_terms=a.laplacian, neg_qv=a.neg_qv)
         net, scale = r.pop("net"), r.pop("scale")
         state = net.state_dict()
         nets["32"] = {"net": state, "scale": {k: v.cpu() for k, v in scale.items()}}
         lines.append(json.dumps(r))
         print(lines[-1], flush=True)
     if a.case in ("128", "both"):
-        r = experiment_large(net_state=state, iters=a.iters_large, lr=a.lr, sprints=a.sprints)
+        r = experiment_large(net_state=state, iters=a.iters_large, lr=a.lr, sprints=a.sprints,
+                             laplacian_terms=a.laplacian, neg_qv=a.neg_qv)
         net, scale = r.pop("net"), r.pop("scale")
         nets["128"] = {"net": net.state_dict(), "scale": {k: v.cpu() for k, v in scale.items()}}
         lines.append(json.dumps(r))
