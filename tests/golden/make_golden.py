@@ -20,6 +20,11 @@ Cases
                    pi' on the interior, stored as FP32.
   base_option1.npz the reference's own option-1 base state (setup_lex.py:74-146) columns,
                    pinning the hydrostatic integration of oracle/ic.py.
+  dl_packing.npz   the learned correction's interface on a 16x12x8 grid: the network input the
+                   reference's phys_state_tuple2array (dl_models.py:125-155) makes from a random
+                   padded state and keepdims scaling_params, and the correction it applies
+                   (correct_array2tuple + the scaling of one_sprint_functions.py:139-143) for a
+                   random network output; output ranges vary with height only (w's not at all).
 """
 import os
 import sys
@@ -152,11 +157,58 @@ def case_base(R, out):
                         rho0_theta0=np.asarray(rho0_theta0)[0, 0])
 
 
+def case_dl(R, ref_dir, out):
+    """dl_models.py run under the stand-in: flax.linen and zarr are only needed for its class
+    definitions and imports, so minimal stubs stand in for them."""
+    import importlib.util
+    import types
+    linen = types.ModuleType("flax.linen")
+    linen.Module = type("Module", (), {})
+    linen.compact = lambda f: f
+    flax = types.ModuleType("flax")
+    flax.linen = linen
+    sys.modules.setdefault("flax", flax)
+    sys.modules.setdefault("flax.linen", linen)
+    sys.modules.setdefault("zarr", types.ModuleType("zarr"))
+    jnp = sys.modules["jax.numpy"]
+    jnp.stack = np.stack
+    jnp.unstack = np.unstack
+    spec = importlib.util.spec_from_file_location("dl_models_reference", os.path.join(ref_dir, "dl_models.py"))
+    dlm = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(dlm)
+    nl = R.nl
+    nx, ny, nz, dx, dy, dz, dt = 16, 12, 8, 600.0, 500.0, 300.0, 3.0
+    set_namelist(nl, nx, ny, nz, dx, dy, dz, dt)
+    js.set_dtype(np.float64)
+    phys, _, _ = WarmBubble(nx, ny, nz, dx, dy, dz).build()
+    state = random_state(phys, nx, ny, nz, seed=21)
+    rng = np.random.default_rng(22)
+    interior = lambda a, e: np.asarray(a)[3:3 + nx + e[0], 3:3 + ny + e[1], 1:1 + nz + e[2]]
+    scaling = []
+    for f, (a, e) in enumerate(zip((state[0], state[1], state[2], state[3], state[5]),
+                                   ((0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (0, 0, 0)))):
+        x = interior(a, e)
+        lo = x - rng.uniform(0.1, 0.5, size=x.shape)
+        rng_z = rng.uniform(0.5, 2.0, size=x.shape[2])          # output range: per level only,
+        if f == 3:                                              # and for w the same on every level
+            rng_z[:] = rng_z[0]
+        scaling += [lo[None, None], (lo + rng_z[None, None, :])[None, None]]
+    scaling += [np.zeros((1, 1, nx, ny, nz))] * 4               # Laplacian ranges (unused here)
+    packed = np.asarray(dlm.phys_state_tuple2array(tuple(np.asarray(a) for a in state), tuple(scaling)))
+    corr = rng.normal(size=(nx, ny, nz, 5))
+    th_c, u_c, v_c, w_c, q_c = (np.asarray(a) for a in dlm.correct_array2tuple(corr))
+    mm = [(scaling[2 * f + 1] - scaling[2 * f]).squeeze() for f in range(5)]
+    np.savez(out, nx=nx, ny=ny, nz=nz, **{"in_" + f: np.asarray(a) for f, a in zip(FIELDS, state)},
+             **{"sc_%d" % i: a for i, a in enumerate(scaling[:10])}, packed=packed, corr=corr,
+             out_theta=th_c * mm[0], out_u=u_c * mm[1], out_v=v_c * mm[2], out_w=w_c * mm[3], out_qv=q_c * mm[4])
+
+
 def main(ref_dir):
     R = js.load_reference(ref_dir)
     case_ops(R, os.path.join(HERE, "ops_random.npz"))
     case_bubble(R, os.path.join(HERE, "bubble_steps.npz"))
     case_base(R, os.path.join(HERE, "base_option1.npz"))
+    case_dl(R, ref_dir, os.path.join(HERE, "dl_packing.npz"))
     if "--long" in sys.argv:
         case_bubble_600s(R, os.path.join(HERE, "bubble32_600s.npz"))
 
