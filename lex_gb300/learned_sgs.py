@@ -88,14 +88,20 @@ def coarse_solver(dims=(32, 32, 32), spacing=(600., 600., 300.), dt=3.0):
 
 
 def laplacian(a, spacing):
-    """7-point Laplacian of a cell field [nz][ny][nx]: periodic in x and y, zero gradient through
-    the bottom and the lid (laplace_of_tensor, dataset_generation.py:291-317)."""
+    """7-point Laplacian of a cell field [nz][ny][nx] as the training loss computes it
+    (laplace_of_tensor_jnp, dataset_generation.py:320-347): periodic in x and y, the end levels
+    copied in z (zero gradient through the bottom and the lid), and no vertical term in the first
+    and last x columns - the reference zeroes s_z[:, :, 0] and s_z[:, :, -1] of its
+    [sequence][step][x][y][z] arrays (:334-335), whose third index is x."""
     dx, dy, dz = spacing
     lx = (torch.roll(a, -1, 2) - 2.0 * a + torch.roll(a, 1, 2)) / (dx * dx)
     ly = (torch.roll(a, -1, 1) - 2.0 * a + torch.roll(a, 1, 1)) / (dy * dy)
     z = torch.zeros_like(a[:1])
     gz = torch.cat([z, (a[1:] - a[:-1]) / dz, z], 0)
-    return lx + ly + (gz[1:] - gz[:-1]) / dz
+    keep = torch.ones(a.shape[2], dtype=a.dtype, device=a.device)
+    keep[0] = 0.0
+    keep[-1] = 0.0
+    return lx + ly + (gz[1:] - gz[:-1]) / dz * keep
 
 
 def field_scale(snapshots, spacing=None):

@@ -24,7 +24,9 @@ Cases
                    reference's phys_state_tuple2array (dl_models.py:125-155) makes from a random
                    padded state and keepdims scaling_params, and the correction it applies
                    (correct_array2tuple + the scaling of one_sprint_functions.py:139-143) for a
-                   random network output; output ranges vary with height only (w's not at all).
+                   random network output; output ranges vary with height only (w's not at all);
+                   and the Laplacian of the training loss (dataset_generation.py:320-347) of a
+                   random cell field.
 """
 import os
 import sys
@@ -180,7 +182,7 @@ def case_dl(R, ref_dir, out):
     nx, ny, nz, dx, dy, dz, dt = 16, 12, 8, 600.0, 500.0, 300.0, 3.0
     set_namelist(nl, nx, ny, nz, dx, dy, dz, dt)
     js.set_dtype(np.float64)
-    phys, _, _ = WarmBubble(nx, ny, nz, dx, dy, dz).build()
+    phys, _, grids = WarmBubble(nx, ny, nz, dx, dy, dz).build()
     state = random_state(phys, nx, ny, nz, seed=21)
     rng = np.random.default_rng(22)
     interior = lambda a, e: np.asarray(a)[3:3 + nx + e[0], 3:3 + ny + e[1], 1:1 + nz + e[2]]
@@ -195,12 +197,22 @@ def case_dl(R, ref_dir, out):
         scaling += [lo[None, None], (lo + rng_z[None, None, :])[None, None]]
     scaling += [np.zeros((1, 1, nx, ny, nz))] * 4               # Laplacian ranges (unused here)
     packed = np.asarray(dlm.phys_state_tuple2array(tuple(np.asarray(a) for a in state), tuple(scaling)))
+    # the Laplacian of the training loss (dataset_generation.py:320-347) on a random cell field
+    jnp.copy = js._simple(np.copy)
+    spec = importlib.util.spec_from_file_location("dataset_generation_reference",
+                                                  os.path.join(ref_dir, "dataset_generation.py"))
+    dgen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(dgen)
+    x3d, y3d, z3d, x3d4u, y3d4v, z3d4w = (np.asarray(a) for a in grids[:6])
+    lap_in = rng.normal(size=(1, 1, nx, ny, nz))
+    lap_out = np.asarray(dgen.laplace_of_tensor_jnp(x3d, x3d4u, y3d, y3d4v, z3d, z3d4w, js._cast_tree(lap_in)))
     corr = rng.normal(size=(nx, ny, nz, 5))
     th_c, u_c, v_c, w_c, q_c = (np.asarray(a) for a in dlm.correct_array2tuple(corr))
     mm = [(scaling[2 * f + 1] - scaling[2 * f]).squeeze() for f in range(5)]
     np.savez(out, nx=nx, ny=ny, nz=nz, **{"in_" + f: np.asarray(a) for f, a in zip(FIELDS, state)},
              **{"sc_%d" % i: a for i, a in enumerate(scaling[:10])}, packed=packed, corr=corr,
-             out_theta=th_c * mm[0], out_u=u_c * mm[1], out_v=v_c * mm[2], out_w=w_c * mm[3], out_qv=q_c * mm[4])
+             out_theta=th_c * mm[0], out_u=u_c * mm[1], out_v=v_c * mm[2], out_w=w_c * mm[3], out_qv=q_c * mm[4],
+             lap_in=lap_in[0, 0], lap_out=lap_out[0, 0], spacing=np.array([dx, dy, dz]))
 
 
 def main(ref_dir):

@@ -95,24 +95,15 @@ def test_bubble_generators():
     assert one[0][2:] == (9600.0, 9600.0)
 
 
-def test_laplacian_matches_the_reference_stencil():
+def test_laplacian_matches_the_reference():
+    """Against the reference's own laplace_of_tensor_jnp (tests/golden/dl_packing.npz)."""
     import numpy as np
+    from conftest import load_golden
     from lex_gb300.learned_sgs import laplacian
-    a = torch.rand(5, 4, 6, dtype=torch.float64, generator=torch.Generator().manual_seed(9))
-    dx, dy, dz = 2.0, 3.0, 0.5
-    # restatement of laplace_of_tensor on [x][y][z]: periodic x, y; end levels copied in z and
-    # the end vertical gradients zeroed
-    s = a.numpy().transpose(2, 1, 0)
-    p = np.concatenate((s[-1:], s, s[:1]), 0)
-    p = np.concatenate((p[:, -1:], p, p[:, :1]), 1)
-    p = np.concatenate((p[:, :, :1], p, p[:, :, -1:]), 2)
-    sx = (p[1:, 1:-1, 1:-1] - p[:-1, 1:-1, 1:-1]) / dx
-    sy = (p[1:-1, 1:, 1:-1] - p[1:-1, :-1, 1:-1]) / dy
-    sz = (p[1:-1, 1:-1, 1:] - p[1:-1, 1:-1, :-1]) / dz
-    sz[:, :, 0] = 0.0
-    sz[:, :, -1] = 0.0
-    ref = (sx[1:] - sx[:-1]) / dx + (sy[:, 1:] - sy[:, :-1]) / dy + (sz[:, :, 1:] - sz[:, :, :-1]) / dz
-    assert np.allclose(laplacian(a, (dx, dy, dz)).numpy().transpose(2, 1, 0), ref, rtol=1e-12, atol=1e-12)
+    g = load_golden("dl_packing.npz")
+    a = torch.tensor(np.ascontiguousarray(g["lap_in"].transpose(2, 1, 0)))
+    got = laplacian(a, tuple(float(v) for v in g["spacing"])).numpy().transpose(2, 1, 0)
+    assert np.allclose(got, g["lap_out"], rtol=1e-12, atol=1e-15)
 
 
 def test_loss_options():
