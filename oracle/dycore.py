@@ -17,6 +17,7 @@ Reference correspondence (file:line):
   advection_pi .......................... advection.py:152-197
   get_divergence / get_divergence2 ...... advection.py:200-236
   pressure_gradient_force ............... pressure_gradient_coriolis.py:7-37
+  calculate_coriolis_force (+ _with_lspgrad) pressure_gradient_coriolis.py:80-113
   calculate_buoyancy .................... pressure_equations.py:123-172
   Smagorinsky ........................... turbulence.py:9-111, :298-446, :474-504
   acoustic sub-steps .................... one_step_integration.py:519-556 / :638-675 / :757-794
@@ -25,6 +26,7 @@ Reference correspondence (file:line):
   Wicker-Skamarock RK3 big step ......... one_sprint_functions.py:10-30
 """
 import numpy as np
+from . import xp
 from .ic import NGX, NGY, NGZ, RD, CP, CV, G, REPS, REPSM1, pad_scalar, pad_u, pad_v
 
 WEPS_MOM = 1.0e-16     # one_step_integration.py:896
@@ -48,10 +50,10 @@ def weno5(a, b, c, d, e, eps):
     b1 = (13.0 / 12.0) * (a - 2.0 * b + c) ** 2 + 0.25 * (a - 4.0 * b + 3.0 * c) ** 2
     b2 = (13.0 / 12.0) * (b - 2.0 * c + d) ** 2 + 0.25 * (b - d) ** 2
     b3 = (13.0 / 12.0) * (c - 2.0 * d + e) ** 2 + 0.25 * (3.0 * c - 4.0 * d + e) ** 2
-    tau = np.abs(b1 - b3)
-    w1 = 0.1 * (1.0 + np.fmin(1.0e30, tau / (b1 + eps)) ** 2)
-    w2 = 0.6 * (1.0 + np.fmin(1.0e30, tau / (b2 + eps)) ** 2)
-    w3 = 0.3 * (1.0 + np.fmin(1.0e30, tau / (b3 + eps)) ** 2)
+    tau = abs(b1 - b3)
+    w1 = 0.1 * (1.0 + xp.fmin(1.0e30, tau / (b1 + eps)) ** 2)
+    w2 = 0.6 * (1.0 + xp.fmin(1.0e30, tau / (b2 + eps)) ** 2)
+    w3 = 0.3 * (1.0 + xp.fmin(1.0e30, tau / (b3 + eps)) ** 2)
     q1 = (2.0 / 6.0) * a + (-7.0 / 6.0) * b + (11.0 / 6.0) * c
     q2 = (-1.0 / 6.0) * b + (5.0 / 6.0) * c + (2.0 / 6.0) * d
     q3 = (2.0 / 6.0) * c + (5.0 / 6.0) * d + (-1.0 / 6.0) * e
@@ -62,9 +64,9 @@ def weno3(a, b, c, eps):
     """Upwind WENO3 value at the face right of ``b``; a, b, c = s[-1], s[0], s[+1] (advection.py:327-337)."""
     b1 = (a - b) ** 2
     b2 = (b - c) ** 2
-    tau = np.abs(b1 - b2)
-    w1 = (1.0 / 3.0) * (1.0 + np.fmin(1.0e30, tau / (b1 + eps)) ** 2)
-    w2 = (2.0 / 3.0) * (1.0 + np.fmin(1.0e30, tau / (b2 + eps)) ** 2)
+    tau = abs(b1 - b2)
+    w1 = (1.0 / 3.0) * (1.0 + xp.fmin(1.0e30, tau / (b1 + eps)) ** 2)
+    w2 = (2.0 / 3.0) * (1.0 + xp.fmin(1.0e30, tau / (b2 + eps)) ** 2)
     return (w1 * ((-1.0 / 2.0) * a + (3.0 / 2.0) * b) + w2 * ((1.0 / 2.0) * b + (1.0 / 2.0) * c)) / (w1 + w2)
 
 
@@ -95,19 +97,19 @@ def recon_vertical(s, eps):
     N = s.shape[2]
     nf = N - 1
     lv = lambda k: s[:, :, k:k + 1]
-    up = np.zeros(s.shape[:2] + (nf,), dtype=s.dtype)
-    dn = np.zeros_like(up)
+    up = xp.zeros(tuple(s.shape[:2]) + (nf,), like=s)
+    dn = xp.zeros_like(up)
     # upward (w >= 0): centred at face 1, WENO3 at face 2 and face nf-2, WENO5 in between
     up[:, :, 1:2] = 0.5 * (lv(1) + lv(2))
     up[:, :, 2:3] = weno3(lv(1), lv(2), lv(3), eps)
-    f = np.arange(3, nf - 2)
-    if f.size:
+    f = xp.arange(3, nf - 2, like=s)
+    if xp.size(f):
         up[:, :, 3:nf - 2] = weno5(s[:, :, f - 2], s[:, :, f - 1], s[:, :, f], s[:, :, f + 1], s[:, :, f + 2], eps)
     up[:, :, nf - 2:nf - 1] = weno3(lv(N - 4), lv(N - 3), lv(N - 2), eps)
     # downward (w < 0): WENO3 at face 1 and face nf-3, centred at face nf-2, WENO5 in between
     dn[:, :, 1:2] = weno3(lv(3), lv(2), lv(1), eps)
-    f = np.arange(2, nf - 3)
-    if f.size:
+    f = xp.arange(2, nf - 3, like=s)
+    if xp.size(f):
         dn[:, :, 2:nf - 3] = weno5(s[:, :, f + 3], s[:, :, f + 2], s[:, :, f + 1], s[:, :, f], s[:, :, f - 1], eps)
     dn[:, :, nf - 3:nf - 2] = weno3(lv(N - 2), lv(N - 3), lv(N - 4), eps)
     dn[:, :, nf - 2:nf - 1] = 0.5 * (lv(N - 2) + lv(N - 3))
@@ -116,7 +118,7 @@ def recon_vertical(s, eps):
 
 def upwind_flux(m, pos, neg):
     """jax.lax.select(m >= 0, m*pos, m*neg): ties go to the positive branch."""
-    return np.where(m >= 0.0, m * pos, m * neg)
+    return xp.where(m >= 0.0, m * pos, m * neg)
 
 
 def col(c):
@@ -133,35 +135,50 @@ class Dycore:
 
     grid: oracle.ic.Grid (uniform dx, dy, dz); base: dict of padded FP64 columns
     theta0, qv0, pi0, rho0 (each (nz+2,)); dt, n_sound; dtype FP64 or FP32.
+    device: None for NumPy arrays; a torch device ("cpu", "cuda") to evaluate the same
+    expressions on torch tensors of that dtype (``cast`` converts a NumPy state).
     """
 
-    def __init__(self, grid, base, dt, n_sound=32, dtype=np.float64, turb=True, cs=CS):
+    def __init__(self, grid, base, dt, n_sound=32, dtype=np.float64, turb=True, cs=CS, cor_opt=0, f_cor=1.0e-4,
+                 device=None):
+        self.device = device
         self.g = grid
         self.cs = cs
+        self.cor_opt = int(cor_opt)
+        self.f_cor = f_cor
         self.nx, self.ny, self.nz = grid.nx, grid.ny, grid.nz
         self.dt = dt
         self.n_sound = n_sound
         self.turb = turb
         self.dtype = np.dtype(dtype).type
-        t = self.dtype
+        if device is None:
+            t = self.dtype
+            arr = lambda a: np.asarray(a, dtype=t)
+        else:
+            import torch
+            tdt = torch.float64 if self.dtype == np.float64 else torch.float32
+            t = float if tdt == torch.float64 else (lambda v: float(np.float32(v)))
+            arr = lambda a: xp.to_torch(a, device, tdt)
+        self._arr = arr
+        self._s = t
         self.dx, self.dy, self.dz = t(grid.dx), t(grid.dy), t(grid.dz)
-        self.theta0 = col(np.asarray(base["theta0"], dtype=t))
-        self.qv0 = col(np.asarray(base["qv0"], dtype=t))
-        self.pi0 = col(np.asarray(base["pi0"], dtype=t))
-        self.rho0 = col(np.asarray(base["rho0"], dtype=t))
+        self.theta0 = col(arr(base["theta0"]))
+        self.qv0 = col(arr(base["qv0"]))
+        self.pi0 = col(arr(base["pi0"]))
+        self.rho0 = col(arr(base["rho0"]))
         # cc1/cc2 of setup_lex.py:25-29 for a uniform grid
         self.cc1 = t(0.5)
         self.cc2 = t(1.0) - self.cc1
 
     def cast(self, state):
-        return tuple(np.asarray(a, dtype=self.dtype) for a in state)
+        return tuple(self._arr(a) for a in state)
 
     # ------------------------------------------------------------------ divergence
     def mass_divergence(self, u, v, w):
         """get_divergence (advection.py:200-226) on the whole padded scalar array."""
         r = self.rho0
-        rw = np.concatenate((np.zeros_like(r[:, :, :1]), 0.5 * (r[:, :, :-1] + r[:, :, 1:]),
-                             np.zeros_like(r[:, :, :1])), axis=2)
+        rw = xp.concat((xp.zeros_like(r[:, :, :1]), 0.5 * (r[:, :, :-1] + r[:, :, 1:]),
+                        xp.zeros_like(r[:, :, :1])), axis=2)
         dvx = (r * u[1:] - r * u[:-1]) / self.dx
         dvy = (r * v[:, 1:] - r * v[:, :-1]) / self.dy
         dvz = (rw[:, :, 1:] * w[:, :, 1:] - rw[:, :, :-1] * w[:, :, :-1]) / self.dz
@@ -289,7 +306,25 @@ class Dycore:
             (pip[IX, IY, 1:] - pip[IX, IY, :-1]) / self.dz)
         pw[:, :, 0] = 0.0
         pw[:, :, -1] = 0.0
+        if xp.is_torch(pu):
+            return pu, pv, pw
         return pu.astype(self.dtype), pv.astype(self.dtype), pw.astype(self.dtype)
+
+    def coriolis(self, u, v):
+        """calculate_coriolis_force / calculate_coriolis_force_with_lspgrad (pressure_gradient_coriolis.py:80-113).
+
+        Returns (fu at v points (nx, ny+1, nz), fv at u points (nx+1, ny, nz)): four-point averages of
+        the other wind times f; cor_opt 2 subtracts a 1 m/s geostrophic wind from u's average.
+        """
+        nx, ny = self.nx, self.ny
+        f = self._s(self.f_cor)
+        fv = 0.25 * (v[2:nx + 3, 3:ny + 3, IZ] + v[2:nx + 3, 4:ny + 4, IZ]
+                     + v[3:nx + 4, 3:ny + 3, IZ] + v[3:nx + 4, 4:ny + 4, IZ])
+        fu = 0.25 * (u[3:nx + 3, 2:ny + 3, IZ] + u[3:nx + 3, 3:ny + 4, IZ]
+                     + u[4:nx + 4, 2:ny + 3, IZ] + u[4:nx + 4, 3:ny + 4, IZ])
+        if self.cor_opt == 2:
+            return f * (fu - 1.0), f * (fv - 0.0)
+        return f * fu, f * fv
 
     @staticmethod
     def extrapolate_ends(a):
@@ -301,13 +336,13 @@ class Dycore:
     def to_w(self, a):
         """interpolate_scalar2w (pressure_equations.py:123-128) on an interior array."""
         bot, top = self.extrapolate_ends(a)
-        return np.concatenate((bot, 0.5 * (a[:, :, :-1] + a[:, :, 1:]), top), axis=2)
+        return xp.concat((bot, 0.5 * (a[:, :, :-1] + a[:, :, 1:]), top), axis=2)
 
     @staticmethod
     def to_w0(a):
         """interpolate_scalar2w_0 (pressure_equations.py:131-138): zero at the end faces."""
-        z = np.zeros_like(a[:, :, :1])
-        return np.concatenate((z, 0.5 * (a[:, :, :-1] + a[:, :, 1:]), z), axis=2)
+        z = xp.zeros_like(a[:, :, :1])
+        return xp.concat((z, 0.5 * (a[:, :, :-1] + a[:, :, 1:]), z), axis=2)
 
     def buoyancy(self, theta, qv):
         """calculate_buoyancy (pressure_equations.py:162-172) -> (b at scalars, b at w faces)."""
@@ -333,7 +368,7 @@ class Dycore:
         dwdx = (w[3:nx + 4, IY, 2:-2] - w[2:nx + 3, IY, 2:-2]) / dx
         e13 = 0.5 * (dudz + dwdx)
         b0, t0 = self.extrapolate_ends(e13)
-        s13 = np.concatenate((0.5 * (b0[1:] + b0[:-1]),
+        s13 = xp.concat((0.5 * (b0[1:] + b0[:-1]),
                               0.25 * (e13[:-1, :, :-1] + e13[1:, :, 1:] + e13[:-1, :, 1:] + e13[1:, :, :-1]),
                               0.5 * (t0[1:] + t0[:-1])), axis=2)
         s13 = r * s13
@@ -341,7 +376,7 @@ class Dycore:
         dwdy = (w[IX, 3:ny + 4, 2:-2] - w[IX, 2:ny + 3, 2:-2]) / dy
         e23 = 0.5 * (dvdz + dwdy)
         b0, t0 = self.extrapolate_ends(e23)
-        s23 = np.concatenate((0.5 * (b0[:, 1:] + b0[:, :-1]),
+        s23 = xp.concat((0.5 * (b0[:, 1:] + b0[:, :-1]),
                               0.25 * (e23[:, :-1, :-1] + e23[:, 1:, 1:] + e23[:, :-1, 1:] + e23[:, 1:, :-1]),
                               0.5 * (t0[:, 1:] + t0[:, :-1])), axis=2)
         s23 = r * s23
@@ -351,16 +386,16 @@ class Dycore:
     def brunt_vaisala(self, theta, qv):
         """compute_nm (turbulence.py:391-427): N^2 from log(theta*(1+repsm1*qv)), padded."""
         tr = theta * (1.0 + REPSM1 * qv)
-        n28w = np.log(tr[IX, IY, 2:-1] / tr[IX, IY, 1:-2]) / self.dz * G
+        n28w = xp.log(tr[IX, IY, 2:-1] / tr[IX, IY, 1:-2]) / self.dz * G
         bot, top = self.extrapolate_ends(n28w)
-        return pad_scalar(np.concatenate((bot, 0.5 * (n28w[:, :, :-1] + n28w[:, :, 1:]), top), axis=2))
+        return pad_scalar(xp.concat((bot, 0.5 * (n28w[:, :, :-1] + n28w[:, :, 1:]), top), axis=2))
 
     def eddy_coefficients(self, s2, n2):
         """compute_k (turbulence.py:430-446)."""
         delta = np.cbrt(self.dx * self.dy * self.dz)
         s2n2 = s2 - n2 / PRANDTL
-        s2n2 = np.where(s2n2 > 0.0, s2n2, 0.0)
-        km = (self.cs * delta) ** 2 * np.sqrt(s2n2)
+        s2n2 = xp.where(s2n2 > 0.0, s2n2, xp.zeros_like(s2n2))
+        km = (self.cs * delta) ** 2 * xp.sqrt(s2n2)
         return km, km / PRANDTL
 
     def smagorinsky(self, theta, u, v, w, qv):
@@ -393,7 +428,7 @@ class Dycore:
         d33 = (t33[IX, IY, 1:] - t33[IX, IY, :-1]) / dz
         d13x = self.to_w0((t13[4:nx + 4, IY, IZ] - t13[2:nx + 2, IY, IZ]) / (2.0 * dx))
         d23y = self.to_w0((t23[IX, 4:ny + 4, IZ] - t23[IX, 2:ny + 2, IZ]) / (2.0 * dy))
-        r8w = self.to_w(np.broadcast_to(r[:, :, IZ], (nx, ny, self.nz)))
+        r8w = self.to_w(xp.broadcast_to(r[:, :, IZ], (nx, ny, self.nz)))
         sgs_w = -(d13x + d23y + d33) / r8w
         sgs_w[:, :, 0] = 0.0
         sgs_w[:, :, -1] = 0.0
@@ -450,12 +485,16 @@ class Dycore:
         au = self.advect_u(u, v, w, div)
         av = self.advect_v(u, v, w, div)
         aw = self.advect_w(u, v, w, div)
+        if self.cor_opt:
+            # one_step_integration.py:83-86, :127-132: rhs_u = adv4u + fv (+ sgs), rhs_v = adv4v - fu (+ sgs)
+            fu, fv = self.coriolis(u, v)
+            au, av = au + fv, av - fu
         if sgs is not None:
             rhs_u, rhs_v, rhs_w = au + sgs[0], av + sgs[1], aw + b8w + sgs[2]
         else:
             rhs_u, rhs_v, rhs_w = au, av, aw + b8w
         trho = th * (1.0 + REPS * q) / (1.0 + q)
-        dtau = self.dtype(self._dtau(dts, n_sound))
+        dtau = self._s(self._dtau(dts, n_sound))
         un, vn, wn, pn = self.acoustic(u0, v0, w0, p0, pis, rhs_u, rhs_v, rhs_w, trho, n_sound, dtau)
         dth = self.advect_scalar(th, u, v, w, div, WEPS_THETA)
         dq = self.advect_scalar(q, u, v, w, div, WEPS_QV)
@@ -489,7 +528,7 @@ class Dycore:
         xs = xi0
         stages = []
         for dts, n in self.stage_plan():
-            xs, tends = self.stage(xi0, xs, self.dtype(dts), sgs, n)
+            xs, tends = self.stage(xi0, xs, self._s(dts), sgs, n)
             stages.append((xs, tends))
         if return_stages:
             return xs, tends, stages, sgs

@@ -22,6 +22,7 @@ reproduced by ``reference_option1_base_state`` to pin the base-state formulas.
 """
 from dataclasses import dataclass, field
 import numpy as np
+from .xp import concat
 
 NGX, NGY, NGZ = 3, 3, 1
 
@@ -79,23 +80,23 @@ class Grid:
 
 def pad_scalar(a):
     """padding3_array (one_step_integration.py:950-959): periodic x/y, z ghost = edge copy."""
-    a = np.concatenate((a[-NGX:], a, a[:NGX]), axis=0)
-    a = np.concatenate((a[:, -NGY:], a, a[:, :NGY]), axis=1)
-    return np.concatenate((a[:, :, :1], a, a[:, :, -1:]), axis=2)
+    a = concat((a[-NGX:], a, a[:NGX]), axis=0)
+    a = concat((a[:, -NGY:], a, a[:, :NGY]), axis=1)
+    return concat((a[:, :, :1], a, a[:, :, -1:]), axis=2)
 
 
 def pad_u(a):
     """padding3u_array (one_step_integration.py:962-972): the duplicated periodic face is skipped."""
-    a = np.concatenate((a[-(NGX + 1):-1], a, a[1:NGX + 1]), axis=0)
-    a = np.concatenate((a[:, -NGY:], a, a[:, :NGY]), axis=1)
-    return np.concatenate((a[:, :, :1], a, a[:, :, -1:]), axis=2)
+    a = concat((a[-(NGX + 1):-1], a, a[1:NGX + 1]), axis=0)
+    a = concat((a[:, -NGY:], a, a[:, :NGY]), axis=1)
+    return concat((a[:, :, :1], a, a[:, :, -1:]), axis=2)
 
 
 def pad_v(a):
     """padding3v_array (one_step_integration.py:975-985)."""
-    a = np.concatenate((a[-NGX:], a, a[:NGX]), axis=0)
-    a = np.concatenate((a[:, -(NGY + 1):-1], a, a[:, 1:NGY + 1]), axis=1)
-    return np.concatenate((a[:, :, :1], a, a[:, :, -1:]), axis=2)
+    a = concat((a[-NGX:], a, a[:NGX]), axis=0)
+    a = concat((a[:, -(NGY + 1):-1], a, a[:, 1:NGY + 1]), axis=1)
+    return concat((a[:, :, :1], a, a[:, :, -1:]), axis=2)
 
 
 def random_state(phys, nx, ny, nz, seed):

@@ -1,8 +1,8 @@
 """Generate golden vectors by running the reference's own source (LEX) under the NumPy jax stand-in.
 
-Run in a container that has the reference checkout (read-only) at REF_DIR:
+Run in a container that has the reference checkout (read-only); its path is the required argument:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference [--long]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py REF_DIR [--cases ...] [--long]
 
 Writes tests/golden/*.npz.  The fixtures pin the oracle (oracle/dycore.py, oracle/ic.py)
 to the reference, and feed the GPU parity tests; nothing at test time reads the reference.
@@ -215,16 +215,249 @@ def case_dl(R, ref_dir, out):
              lap_in=lap_in[0, 0], lap_out=lap_out[0, 0], spacing=np.array([dx, dy, dz]))
 
 
-def main(ref_dir):
-    R = js.load_reference(ref_dir)
-    case_ops(R, os.path.join(HERE, "ops_random.npz"))
-    case_bubble(R, os.path.join(HERE, "bubble_steps.npz"))
-    case_base(R, os.path.join(HERE, "base_option1.npz"))
-    case_dl(R, ref_dir, os.path.join(HERE, "dl_packing.npz"))
-    if "--long" in sys.argv:
-        case_bubble_600s(R, os.path.join(HERE, "bubble32_600s.npz"))
+def case_coriolis(R, out):
+    """One big step of the ops_random state with Coriolis on (cor_opt 1 and 2, f = 1e-4): the three
+    stages' tendencies, the step's result, and the Coriolis terms themselves (pressure_gradient_coriolis.py:80-113)."""
+    nl = R.nl
+    nx, ny, nz, dx, dy, dz, dt = 16, 12, 8, 600.0, 500.0, 300.0, 3.0
+    set_namelist(nl, nx, ny, nz, dx, dy, dz, dt)
+    nl.fCor = 1.0e-4
+    phys, base, grids = WarmBubble(nx, ny, nz, dx, dy, dz).build()
+    state = random_state(phys, nx, ny, nz, seed=11)
+    js.set_dtype(np.float64)
+    c = js._cast_tree
+    state, base, grids = c(state), c(base), c(grids)
+    d = dict(nx=nx, ny=ny, nz=nz, dx=dx, dy=dy, dz=dz, dt=dt, n_sound=32, f_cor=nl.fCor, **columns(base))
+    for k, a in zip(FIELDS, state):
+        d["in_" + k] = np.asarray(a)
+    tnames = ("dtheta", "dpip", "du", "dv", "dw", "dqv")
+    for cor in (1, 2):
+        mo = (2, False, False, cor, False, False, 1)
+        f = R.pres_grad.calculate_coriolis_force if cor == 1 else R.pres_grad.calculate_coriolis_force_with_lspgrad
+        fu, fv = f(state[1], state[2])
+        d["cor%d_fu" % cor], d["cor%d_fv" % cor] = fu, fv
+        xi1, t1, sfc, heat, sgs_t = R.one.rk_sub_step0(state, state, base, grids, mo, nl.dt / 3.0)
+        xi2, t2 = R.one.rk_sub_step1(state, xi1, base, grids, heat, sfc, sgs_t, mo, nl.dt / 2.0)
+        xi3, t3 = R.one.rk_sub_step2(state, xi2, base, grids, heat, sfc, sgs_t, mo, nl.dt)
+        for s, tt in enumerate((t1, t2, t3)):
+            for k, a in zip(tnames, tt):
+                d["cor%d_stage%d_%s" % (cor, s, k)] = a
+        for k, a in zip(FIELDS, xi3):     # the big step's result (padded)
+            d["cor%d_step_%s" % (cor, k)] = a
+    nl.fCor = 1.0e-4
+    np.savez_compressed(out, **{k: np.asarray(v) for k, v in d.items()})
+
+
+# ---------------------------------------------------------------------------------------------------------
+# the 100 m warm bubble on 192 x 192 x 96 (dt = 1 s): reduced records, since whole fields would be ~14 MB each
+# ---------------------------------------------------------------------------------------------------------
+BIG = dict(nx=192, ny=192, nz=96, dx=100.0, dy=100.0, dz=100.0, dt=1.0)
+NSAMPLE = 4096
+
+
+def sample_index(shape, seed=7):
+    """Seeded flat indices (C order) of NSAMPLE points of an array of ``shape``."""
+    n = int(np.prod(shape))
+    return np.sort(np.random.default_rng(seed + n % 9973).choice(n, NSAMPLE, replace=False))
+
+
+def reduce_into(d, key, a):
+    """FP64 summary of a whole interior field: L2 norm, sum, max |.|, and the values at seeded points."""
+    a = np.asarray(a, dtype=np.float64)
+    d[key + "_norm"] = np.linalg.norm(a)
+    d[key + "_sum"] = a.sum()
+    d[key + "_amax"] = np.abs(a).max()
+    d[key + "_idx"] = sample_index(a.shape)
+    d[key + "_at"] = a.reshape(-1)[d[key + "_idx"]]
+
+
+def _np(a):
+    return a.detach().cpu().numpy() if hasattr(a, "detach") else np.asarray(a)
+
+
+def case_bubble192_step(R, out):
+    """One WS-RK3 big step of the 192 x 192 x 96 warm bubble (FP64, NumPy stand-in): per stage, the six
+    tendencies (rk_sub_step0/1/2's tuple) and the six interior stage fields, each reduced."""
+    nl = R.nl
+    g = BIG
+    set_namelist(nl, g["nx"], g["ny"], g["nz"], g["dx"], g["dy"], g["dz"], g["dt"])
+    wb = WarmBubble(g["nx"], g["ny"], g["nz"], g["dx"], g["dy"], g["dz"])
+    phys, base, grids = wb.build()
+    js.set_dtype(np.float64)
+    c = js._cast_tree
+    state, base, grids = c(phys), c(base), c(grids)
+    d = dict(seed=wb.seed, **g)
+    xi1, t1, sfc, heat, sgs_t = R.one.rk_sub_step0(state, state, base, grids, MODEL_OPT, nl.dt / 3.0)
+    xi2, t2 = R.one.rk_sub_step1(state, xi1, base, grids, heat, sfc, sgs_t, MODEL_OPT, nl.dt / 2.0)
+    xi3, t3 = R.one.rk_sub_step2(state, xi2, base, grids, heat, sfc, sgs_t, MODEL_OPT, nl.dt)
+    tnames = ("dtheta", "dpip", "du", "dv", "dw", "dqv")
+    inner = {"theta": (slice(3, -3), slice(3, -3), slice(1, -1)), "u": (slice(3, -3), slice(3, -3), slice(1, -1)),
+             "v": (slice(3, -3), slice(3, -3), slice(1, -1)), "w": (slice(3, -3), slice(3, -3), slice(1, -1)),
+             "pip": (slice(3, -3), slice(3, -3), slice(1, -1)), "qv": (slice(3, -3), slice(3, -3), slice(1, -1))}
+    for s, (xi, tt) in enumerate(((xi1, t1), (xi2, t2), (xi3, t3))):
+        for k, a in zip(tnames, tt):
+            reduce_into(d, "stage%d_%s" % (s, k), a)
+        for k, a in zip(FIELDS, xi):
+            a = np.asarray(a)[inner[k]]
+            reduce_into(d, "stage%d_%s" % (s, k), a - 300.0 if k == "theta" else a)
+    np.savez_compressed(out, **{k: np.asarray(v) for k, v in d.items()})
+
+
+def case_bubble192_600s(R, jt, out, checkpoint=None, nsteps=600):
+    """600 s (600 RK3 steps) of the 192 x 192 x 96 warm bubble under the torch stand-in (FP64): norms at
+    60, 300 and 600 s, and at 600 s the x-z plane through the bubble centre (j = 96) and every 4th point
+    of theta - 300 K, qv - qv0, w and pi' (FP32).  Resumable from ``checkpoint`` (a state file)."""
+    import time
+    import torch
+    nl = R.nl
+    g = BIG
+    set_namelist(nl, g["nx"], g["ny"], g["nz"], g["dx"], g["dy"], g["dz"], g["dt"])
+    wb = WarmBubble(g["nx"], g["ny"], g["nz"], g["dx"], g["dy"], g["dz"])
+    phys, base, grids = wb.build()
+    qv0 = base[4][3:-3, 3:-3, 1:-1]
+    st, bt, gt = jt.tree(phys), jt.tree(base), jt.tree(grids)
+    d = dict(seed=wb.seed, nsteps=nsteps, **g)
+    n0 = 0
+    if checkpoint and os.path.exists(checkpoint):
+        with np.load(checkpoint) as z:
+            n0 = int(z["n"])
+            st = tuple(torch.as_tensor(z[k]) for k in FIELDS)
+            d.update({k: z[k] for k in z.files if k[0] == "t" and k[1:2].isdigit()})
+
+    def record(n, st):
+        th, u, v, w, pip, qv = (_np(a) for a in st)
+        inner = (slice(3, -3), slice(3, -3), slice(1, -1))
+        f = {"theta_p": th[inner] - 300.0, "qv_p": qv[inner] - qv0, "w": w[3:-3, 3:-3, 1:-1], "pip": pip[inner],
+             "u": u[3:-3, 3:-3, 1:-1], "v": v[3:-3, 3:-3, 1:-1]}
+        for k, a in f.items():
+            d["t%d_%s_norm" % (n, k)] = np.linalg.norm(a)
+            d["t%d_%s_amax" % (n, k)] = np.abs(a).max()
+        if n == nsteps:
+            for k in ("theta_p", "qv_p", "w", "pip"):
+                d["t%d_%s_xz" % (n, k)] = f[k][:, g["ny"] // 2, :].astype(np.float32)
+                d["t%d_%s_sub4" % (n, k)] = f[k][::4, ::4, ::4].astype(np.float32)
+
+    with torch.no_grad():
+        for n in range(n0 + 1, nsteps + 1):
+            t0 = time.time()
+            st, _ = R.sp.ws_rk3_big_step(st, bt, gt, MODEL_OPT)
+            if n in (60, 300, nsteps):
+                record(n, st)
+            if checkpoint and (n % 20 == 0 or n == nsteps):
+                tmp = checkpoint + ".tmp.npz"
+                np.savez(tmp, n=n, **{k: _np(a) for k, a in zip(FIELDS, st)},
+                         **{k: v for k, v in d.items() if k[0] == "t" and k[1:2].isdigit()})
+                os.replace(tmp, checkpoint)
+            print("step %d %.1f s" % (n, time.time() - t0), flush=True)
+    np.savez_compressed(out, **{k: np.asarray(v) for k, v in d.items()})
+
+
+def case_adjoint(R, jt, out):
+    """torch.autograd through the reference's ws_rk3_big_step (torch stand-in, FP64) as the stand-in for
+    jax.vjp: on the ops_random state (16 x 12 x 8, Smagorinsky on), the adjoint of the interior state for
+    seeded output seeds, after one big step and after a three-step rollout, with cor_opt 0 and 1.
+
+    Inputs and outputs are in the device layout of the library (interior only, x fastest: [z][y][x],
+    u and v without the duplicated periodic face, w on the nz+1 faces): the padding the reference applies
+    to its inputs (padding3*_array) is part of the differentiated function, so its adjoint folds the ghost
+    cells back onto the interior values they copy."""
+    import torch
+    from oracle.ic import pad_scalar, pad_u, pad_v
+    nl = R.nl
+    nx, ny, nz, dx, dy, dz, dt = 16, 12, 8, 600.0, 500.0, 300.0, 3.0
+    set_namelist(nl, nx, ny, nz, dx, dy, dz, dt)
+    nl.fCor = 1.0e-4
+    phys, base, grids = WarmBubble(nx, ny, nz, dx, dy, dz).build()
+    state = random_state(phys, nx, ny, nz, seed=11)
+    bt, gt = jt.tree(base), jt.tree(grids)
+    inner = (slice(3, -3), slice(3, -3), slice(1, -1))
+
+    def to_dev(k, a):   # padded reference array -> device layout [z][y][x]
+        a = a[inner]
+        if k == "u":
+            a = a[:-1]
+        elif k == "v":
+            a = a[:, :-1]
+        return a.permute(2, 1, 0) if hasattr(a, "permute") else np.transpose(a, (2, 1, 0))
+
+    def from_dev(k, a):  # device layout -> padded reference array (differentiable)
+        a = a.permute(2, 1, 0)
+        if k == "u":
+            return pad_u(torch.cat((a, a[:1]), 0))
+        if k == "v":
+            return pad_v(torch.cat((a, a[:, :1]), 1))
+        return pad_scalar(a)
+
+    x0 = [torch.as_tensor(np.ascontiguousarray(to_dev(k, np.asarray(a)))) for k, a in zip(FIELDS, state)]
+    rng = np.random.default_rng(31)
+    ybar = [torch.as_tensor(rng.standard_normal(tuple(x.shape))) for x in x0]
+    ybar[3][0] = 0.0      # w on the bottom and lid faces is zero by construction
+    ybar[3][-1] = 0.0
+    d = dict(nx=nx, ny=ny, nz=nz, dx=dx, dy=dy, dz=dz, dt=dt, n_sound=32, f_cor=nl.fCor, **columns(base))
+    for k, x in zip(FIELDS, x0):
+        d["x_" + k] = x.numpy()
+    for k, y in zip(FIELDS, ybar):
+        d["ybar_" + k] = y.numpy()
+    for cor in (0, 1):
+        mo = (2, False, False, cor, False, False, 1)
+        for nsteps in (1, 3):
+            xs = [x.clone().requires_grad_(True) for x in x0]
+            st = tuple(from_dev(k, x) for k, x in zip(FIELDS, xs))
+            for _ in range(nsteps):
+                st, _ = R.sp.ws_rk3_big_step(st, bt, gt, mo)
+            y = [to_dev(k, a) for k, a in zip(FIELDS, st)]
+            dot = sum((a * b).sum() for a, b in zip(y, ybar))
+            gr = torch.autograd.grad(dot, xs)
+            for k, a, gg in zip(FIELDS, y, gr):
+                d["cor%d_n%d_y_%s" % (cor, nsteps, k)] = a.detach().numpy()
+                d["cor%d_n%d_xbar_%s" % (cor, nsteps, k)] = gg.numpy()
+    np.savez_compressed(out, **{k: np.asarray(v) for k, v in d.items()})
+
+
+FAST = ("ops", "bubble", "base", "dl", "coriolis")
+
+
+def main(argv):
+    import argparse
+    ap = argparse.ArgumentParser(description="golden vectors from the reference's own source")
+    ap.add_argument("ref_dir", help="checkout of the reference (read-only)")
+    ap.add_argument("--cases", default=",".join(FAST),
+                    help="comma-separated: ops, bubble, base, dl, coriolis (fast); bubble32_600s, "
+                         "bubble192_step (about 2 min), bubble192_600s (hours; torch stand-in), adjoint")
+    ap.add_argument("--long", action="store_true", help="also bubble32_600s (the original long case)")
+    ap.add_argument("--checkpoint", default=None, help="bubble192_600s: resumable state file")
+    ap.add_argument("--threads", type=int, default=0, help="torch CPU threads for the torch stand-in cases")
+    a = ap.parse_args(argv)
+    cases = [c for c in a.cases.split(",") if c]
+    if a.long:
+        cases.append("bubble32_600s")
+    torch_cases = [c for c in cases if c in ("bubble192_600s", "adjoint")]
+    numpy_cases = [c for c in cases if c not in torch_cases]
+    if numpy_cases and torch_cases:
+        raise SystemExit("the NumPy and torch stand-ins cannot share a process: run the torch cases separately")
+    if numpy_cases:
+        R = js.load_reference(a.ref_dir)
+        out = lambda n: os.path.join(HERE, n)
+        for c in numpy_cases:
+            {"ops": lambda: case_ops(R, out("ops_random.npz")),
+             "bubble": lambda: case_bubble(R, out("bubble_steps.npz")),
+             "base": lambda: case_base(R, out("base_option1.npz")),
+             "dl": lambda: case_dl(R, a.ref_dir, out("dl_packing.npz")),
+             "coriolis": lambda: case_coriolis(R, out("ops_coriolis.npz")),
+             "bubble32_600s": lambda: case_bubble_600s(R, out("bubble32_600s.npz")),
+             "bubble192_step": lambda: case_bubble192_step(R, out("bubble192_step.npz"))}[c]()
+    if torch_cases:
+        import torch
+        import jax_standin_torch as jt
+        if a.threads:
+            torch.set_num_threads(a.threads)
+        R = jt.load_reference(a.ref_dir)
+        for c in torch_cases:
+            if c == "bubble192_600s":
+                case_bubble192_600s(R, jt, os.path.join(HERE, "bubble192_600s.npz"), a.checkpoint)
+            else:
+                case_adjoint(R, jt, os.path.join(HERE, "adjoint_vjp.npz"))
 
 
 if __name__ == "__main__":
-    args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    main(args[0] if args else "/root/reference")
+    main(sys.argv[1:])

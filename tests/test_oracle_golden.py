@@ -134,3 +134,41 @@ def test_product_workload_matches_oracle_ic():
         np.testing.assert_array_equal(a, b)
     np.testing.assert_array_equal(prof["theta0"], base[2][0, 0])
     np.testing.assert_array_equal(prof["qv0"], base[4][0, 0])
+
+
+def test_coriolis_matches_reference():
+    """calculate_coriolis_force / _with_lspgrad (pressure_gradient_coriolis.py:80-113) and one big step
+    with cor_opt 1 and 2 (f = 1e-4), against the reference run on the ops_random state."""
+    from conftest import load_golden
+    g = load_golden("ops_coriolis.npz")
+    names = ("dtheta", "dpip", "du", "dv", "dw", "dqv")
+    for cor in (1, 2):
+        grid = Grid(int(g["nx"]), int(g["ny"]), int(g["nz"]), float(g["dx"]), float(g["dy"]), float(g["dz"]))
+        base = dict(theta0=g["col_theta0"], qv0=g["col_qv0"], pi0=g["col_pi0"], rho0=g["col_rho0"])
+        D = Dycore(grid, base, float(g["dt"]), int(g["n_sound"]), cor_opt=cor, f_cor=float(g["f_cor"]))
+        fu, fv = D.coriolis(g["in_u"], g["in_v"])
+        assert rel_l2(fu, g["cor%d_fu" % cor]) <= TOL and rel_l2(fv, g["cor%d_fv" % cor]) <= TOL
+        nxt, _, stages, _ = D.step(state_in(g), return_stages=True)
+        for s, (_, tt) in enumerate(stages):
+            for n, a in zip(names, tt):
+                ref = g["cor%d_stage%d_%s" % (cor, s, n)]
+                ref = ref if ref.shape == a.shape else interior_of(ref, n)
+                assert rel_l2(a, ref) <= 1e-12, (cor, s, n)
+        for f, a in zip(FIELDS, nxt):
+            assert rel_l2(a, g["cor%d_step_%s" % (cor, f)]) <= TOL, (cor, f)
+
+
+def test_torch_form_of_the_oracle_matches_numpy(ops_golden):
+    """The oracle's torch form (used for full-size FP64 runs on the GPU) computes what its NumPy form does."""
+    import torch
+    g = ops_golden
+    grid = Grid(int(g["nx"]), int(g["ny"]), int(g["nz"]), float(g["dx"]), float(g["dy"]), float(g["dz"]))
+    base = dict(theta0=g["col_theta0"], qv0=g["col_qv0"], pi0=g["col_pi0"], rho0=g["col_rho0"])
+    for cor in (0, 2):
+        Dn = Dycore(grid, base, float(g["dt"]), int(g["n_sound"]), cor_opt=cor)
+        Dt = Dycore(grid, base, float(g["dt"]), int(g["n_sound"]), cor_opt=cor, device="cpu")
+        a, _ = Dn.step(state_in(g))
+        b, _ = Dt.step(Dt.cast(state_in(g)))
+        for f, x, y in zip(FIELDS, a, b):
+            assert isinstance(y, torch.Tensor)
+            assert rel_l2(y.numpy(), x) <= 1e-14, (cor, f)
