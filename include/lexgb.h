@@ -55,7 +55,15 @@ typedef struct lexgb_config {
     int l2_persist;          /* 0 (default): keep the acoustic sub-steps' per-stage inputs (R_u, R_v, R_w, theta_rho)
                                 in a persisting L2 window; -1: normal caching */
     double cs;               /* Smagorinsky constant; 0 (default): 0.18 (turbulence.py:433) */
+    int acoustic_kernel;     /* how the acoustic sub-steps run: LEXGB_ACOUSTIC_AUTO (0, default: the fastest
+                                form measured for the grid), _ROWS (one launch per sub-step, float4 rows),
+                                _TILE (one launch per sub-step, 32 x 4 x 8 blocks sharing values; nx % 32 == 0,
+                                ny % 4 == 0), _PERSISTENT (stages 1 and 2 as one cooperative launch each, pi' kept
+                                in shared memory, inputs staged by TMA; nx % 32 == 0, ny % 8 == 0, nz <= 99,
+                                a 32 x 8 tile per SM).  A form the grid does not allow falls back to AUTO. */
 } lexgb_config;
+
+enum { LEXGB_ACOUSTIC_AUTO = 0, LEXGB_ACOUSTIC_ROWS = 1, LEXGB_ACOUSTIC_TILE = 2, LEXGB_ACOUSTIC_PERSISTENT = 3 };
 
 typedef struct lexgb_ctx lexgb_ctx;
 
@@ -138,8 +146,22 @@ int lexgb_budget(lexgb_ctx *ctx, double *out, int n_out);
 /* Non-finite check of the state: *n_bad = number of non-finite values (0 = clean). */
 int lexgb_check_finite(lexgb_ctx *ctx, long long *n_bad);
 
-/* Wait for the context's stream. */
+/* Wait for the context's stream.  Returns LEXGB_ERR_TIMEOUT (once, then the status is cleared) when a
+ * bounded device-side wait of the persistent acoustic kernel gave up since the last check; the state is
+ * then invalid and must be uploaded again.  lexgb_download_state, lexgb_check_finite and
+ * lexgb_get_state_interior to host memory report the same status. */
 int lexgb_synchronize(lexgb_ctx *ctx);
+
+/* Polls a grid-barrier wait of the persistent acoustic kernel makes before it gives up with
+ * LEXGB_ERR_TIMEOUT (0: the default, about 2^24 polls of >= 32 ns).  polls < 0 is a test mode: every
+ * grid-barrier wait then waits for one arrival more than there are blocks, so it can only give up,
+ * after -polls polls (the timeout path, without a fault or a hang).  No reference counterpart: the
+ * reference runs each sub-step as separate XLA work (one_step_integration.py:638-675). */
+int lexgb_set_barrier_limit(lexgb_ctx *ctx, long long polls);
+
+/* The acoustic form the context runs (LEXGB_ACOUSTIC_ROWS, _TILE or _PERSISTENT) after AUTO and any
+ * fallback were resolved.  No reference counterpart. */
+int lexgb_acoustic_kernel(lexgb_ctx *ctx, int *kind);
 
 /* Device pointers of the current state in the internal layout (x fastest, interior only,
  * theta stored minus theta_ref, u/v periodic without the duplicated face, w with nz+1 levels). */
@@ -159,6 +181,7 @@ enum {
     LEXGB_KERNEL_SMAG_A,
     LEXGB_KERNEL_SMAG_B,
     LEXGB_KERNEL_ACOUSTIC_PAIR, /* two acoustic sub-steps */
+    LEXGB_KERNEL_ACOUSTIC_STAGE,/* the persistent kernel: all n_sound sub-steps of stage 2 in one launch */
     LEXGB_KERNEL_COUNT
 };
 int lexgb_time_kernel(lexgb_ctx *ctx, int which, int reps, float *ms_per_launch);

@@ -16,7 +16,8 @@ DIAGNOSTICS = ["mass_div", "adv_theta", "adv_qv", "adv_u", "adv_v", "adv_w", "bu
                "pgf_u", "pgf_v", "pgf_w", "adv_pi", "sgs_u", "sgs_v", "sgs_w", "sgs_theta", "sgs_qv",
                "n2", "km"]
 
-KERNELS = ["acoustic", "div_trho", "adv_scalars", "adv_momentum", "smag_a", "smag_b", "acoustic_pair"]
+KERNELS = ["acoustic", "div_trho", "adv_scalars", "adv_momentum", "smag_a", "smag_b", "acoustic_pair",
+           "acoustic_stage"]
 
 # every entry point include/lexgb.h declares: name -> (restype, argtypes)
 _P = ctypes.c_void_p
@@ -30,7 +31,10 @@ class Config(ctypes.Structure):
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
                 ("dt", ctypes.c_double), ("n_sound", ctypes.c_int), ("turb_opt", ctypes.c_int),
                 ("cor_opt", ctypes.c_int), ("f_cor", ctypes.c_double), ("theta_ref", ctypes.c_double),
-                ("acoustic_pairs", ctypes.c_int), ("l2_persist", ctypes.c_int), ("cs", ctypes.c_double)]
+                ("acoustic_pairs", ctypes.c_int), ("l2_persist", ctypes.c_int), ("cs", ctypes.c_double),
+                ("acoustic_kernel", ctypes.c_int)]
+
+ACOUSTIC_KERNELS = {"auto": 0, "rows": 1, "tile": 2, "persistent": 3}
 
 
 SIGNATURES = {
@@ -49,6 +53,8 @@ SIGNATURES = {
     "lexgb_budget": (_I, [_P, _D, _I]),
     "lexgb_check_finite": (_I, [_P, ctypes.POINTER(ctypes.c_longlong)]),
     "lexgb_synchronize": (_I, [_P]),
+    "lexgb_set_barrier_limit": (_I, [_P, ctypes.c_longlong]),
+    "lexgb_acoustic_kernel": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
     "lexgb_state_device_ptrs": (_I, [_P, ctypes.POINTER(_P)]),
     "lexgb_step_kernel_count": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
     "lexgb_time_kernel": (_I, [_P, _I, _I, ctypes.POINTER(ctypes.c_float)]),

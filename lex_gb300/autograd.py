@@ -73,6 +73,7 @@ class _Step(torch.autograd.Function):
             _bind_stream(solver)
             solver.set_cs(float(cs))
         ctx.with_cs = cs is not None
+        ctx.cs = solver.cs      # the backward differentiates the step with this step's Cs
         set_state(solver, state)
         _bind_stream(solver)
         _lib.check(solver.lib.lexgb_step_keep(solver.handle))
@@ -90,6 +91,9 @@ class _Step(torch.autograd.Function):
                    for g, s in zip(grads, _shapes(solver)))
         gx = tuple(torch.empty(s, dtype=torch.float32, device="cuda") for s in _shapes(solver))
         _bind_stream(solver)
+        cs_now = solver.cs
+        if cs_now != ctx.cs:                                    # Cs changed since this step's forward
+            solver.set_cs(ctx.cs)
         if ctx.with_cs:
             solver.cs_grad(reset=True)                          # start this step's accumulation at zero
         if getattr(solver, "_kept_token", None) == ctx.token:   # this step's intermediates are still kept
@@ -98,6 +102,8 @@ class _Step(torch.autograd.Function):
             set_state(solver, ctx.saved_tensors)
             _lib.check(solver.lib.lexgb_step_vjp(solver.handle, 3, _ptrs(gy), _ptrs(gx), 1))
         solver._kept_token = None
+        if solver.cs != cs_now:
+            solver.set_cs(cs_now)
         gcs = torch.tensor(solver.cs_grad(reset=True), dtype=torch.float64, device="cuda") if ctx.with_cs else None
         return (None, gcs) + gx
 

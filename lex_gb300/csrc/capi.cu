@@ -106,6 +106,13 @@ struct lexgb_ctx {
   // persisting L2 window over R_u, R_v, R_w, theta_rho for the acoustic sub-steps
   cudaAccessPolicyWindow l2win{};
   bool l2on = false;
+  // persistent acoustic kernel: blocks (0: not used for this grid), its barrier word and the
+  // sticky device status word (LEXGB_ERR_TIMEOUT after a grid-barrier wait gave up)
+  int persist_blocks = 0;
+  int ak = LEXGB_ACOUSTIC_ROWS;   // the resolved acoustic form
+  unsigned* sync = nullptr;   // [0] barrier arrivals, [1] status
+  long long spin_limit = 1LL << 24;
+  int barrier_test = 0;   // lexgb_set_barrier_limit with polls < 0
   // graph of one big step
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -166,6 +173,13 @@ StagePlan plan_of(const lexgb_config& c) {
   return p;
 }
 
+// one acoustic sub-step with the context's per-sub-step kernel (both give identical results)
+cudaError_t sub_step(lexgb_ctx* c, const AcousticIn& in, const AcousticOut& out, float dtau, int rev,
+                     const cudaAccessPolicyWindow* win) {
+  if (c->ak == LEXGB_ACOUSTIC_TILE) return launch_acoustic_tile(c->d, c->ph, c->cols, in, out, dtau, c->stream, rev, win);
+  return launch_acoustic(c->d, c->ph, c->cols, in, out, dtau, c->stream, rev, win);
+}
+
 int run_smag(lexgb_ctx* c, const State& x, float* n2, float* km) {
   SmagTau t{c->tau[0], c->tau[1], c->tau[2], c->tau[3], c->tau[4], c->tau[5], c->tau[6], n2, km};
   CK(launch_smag_a(c->d, c->ph, c->cols, x, t, c->stream));
@@ -188,9 +202,33 @@ int run_stage(lexgb_ctx* c, int s, const State& xi0, const State& xis, const Sta
   // acoustic_pairs, sub-steps go two per launch (an odd count starts with a single one).
   const int n = p.n[s];
   const float dtau = (float)p.dtau[s];
-  AcousticIn in{xi0.u, xi0.v, xi0.w, xi0.p, c->Ru, c->Rv, c->Rw, c->trho, xis.p};
+  // pi'_s joins the persisting window (R_u, R_v, R_w, theta_rho, then this slot): the divergence
+  // field after theta_rho is free once the advection kernels above have read it
+  const float* ps = xis.p;
+  if (c->l2on && c->l2win.num_bytes >= 5 * c->fstride * sizeof(float) && n > 1) {
+    CK(cudaMemcpyAsync(c->div, xis.p, (size_t)c->d.cells() * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    ps = c->div;
+  }
+  AcousticIn in{xi0.u, xi0.v, xi0.w, xi0.p, c->Ru, c->Rv, c->Rw, c->trho, ps};
   const AcousticOut X{c->Xu, c->Xv, c->Xw, c->Xp}, Y{c->Yu, c->Yv, c->Yw, c->Yp};
   const AcousticOut O{out.u, out.v, out.w, out.p};
+  if (c->persist_blocks > 0 && n >= 2) {  // all sub-steps in one persistent launch (in and out may alias)
+    PersistIO io{};
+    io.u[0] = xi0.u; io.u[1] = c->Xu; io.u[2] = c->Yu; io.u[3] = out.u;
+    io.v[0] = xi0.v; io.v[1] = c->Xv; io.v[2] = c->Yv; io.v[3] = out.v;
+    io.w[0] = xi0.w; io.w[1] = c->Xw; io.w[2] = c->Yw; io.w[3] = out.w;
+    io.p0 = xi0.p; io.po = out.p;
+    io.Ru = c->Ru; io.Rv = c->Rv; io.Rw = c->Rw; io.trho = c->trho; io.ps = ps;
+    io.hb[0] = c->Xp; io.hb[1] = c->Yp;
+    io.bar = c->sync;
+    io.status = reinterpret_cast<int*>(c->sync + 1);
+    io.spin_limit = c->spin_limit;
+    io.unreachable = c->barrier_test;
+    io.nsub = n;
+    io.dtau = dtau;
+    CK(launch_acoustic_persist(c->d, c->ph, c->cols, io, c->stream, c->l2on ? &c->l2win : nullptr));
+    return LEXGB_OK;
+  }
   const bool pairs = c->cfg.acoustic_pairs != 0 && c->d.nx % 4 == 0;  // the pair kernel needs nx % 4 == 0
   const int nsingle = pairs ? (n & 1) : n;
   const int launches = nsingle + (pairs ? n / 2 : 0);
@@ -198,7 +236,7 @@ int run_stage(lexgb_ctx* c, int s, const State& xi0, const State& xis, const Sta
   for (int l = 1; l <= launches; ++l) {
     AcousticOut tgt = (l == launches && !(alias && launches == 1)) ? O : ((l & 1) ? X : Y);
     if (l <= nsingle)
-      CK(launch_acoustic(c->d, c->ph, c->cols, in, tgt, dtau, c->stream, l & 1, c->l2on ? &c->l2win : nullptr));
+      CK(sub_step(c, in, tgt, dtau, l & 1, c->l2on ? &c->l2win : nullptr));
     else
       CK(launch_acoustic_pair(c->d, c->ph, c->cols, in, tgt, dtau, c->stream));
     in.u = tgt.u;
@@ -285,6 +323,20 @@ int check_ready(lexgb_ctx* c) {
   return LEXGB_OK;
 }
 
+// The device status word (after the stream is idle): LEXGB_ERR_TIMEOUT once when a bounded wait of the
+// persistent acoustic kernel gave up, and the word is cleared.
+int take_status(lexgb_ctx* c) {
+  if (!c->sync) return LEXGB_OK;
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, c->sync + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (st == 0) return LEXGB_OK;
+  CK(cudaMemsetAsync(c->sync + 1, 0, sizeof(int), c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return fail(LEXGB_ERR_TIMEOUT, "a grid-barrier wait of the persistent acoustic kernel gave up; the state is "
+                                 "invalid (upload it again)");
+}
+
 int ensure_stage(lexgb_ctx* c, size_t bytes) {
   if (c->stage_bytes >= bytes) return LEXGB_OK;
   if (c->stage) cudaFree(c->stage);
@@ -327,10 +379,11 @@ int build_table(lexgb_ctx* c) {
 
 extern "C" {
 
-// The acoustic sub-steps of a stage all read R_u, R_v, R_w and theta_rho (four adjacent arena
-// fields): a persisting L2 window over them (up to the device's set-aside maximum) keeps them
-// on chip across the 16 or 32 sub-steps, so only the moving state streams through HBM.  The
-// set-aside is a limit of this process's context; failures leave normal caching.
+// The acoustic sub-steps of a stage all read R_u, R_v, R_w, theta_rho and pi'_s (five adjacent arena
+// fields, pi'_s copied into the slot after theta_rho for the stage): a persisting L2 window over
+// them (up to the device's set-aside maximum) keeps them on chip across the 16 or 32 sub-steps, so
+// only the moving state streams through HBM.  The set-aside is a limit of this process's context;
+// failures leave normal caching.
 static void setup_l2_window(lexgb_ctx* c) {
   int dev = 0, max_persist = 0, max_window = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -340,7 +393,7 @@ static void setup_l2_window(lexgb_ctx* c) {
     cudaGetLastError();
     return;
   }
-  size_t bytes = 4 * c->fstride * sizeof(float);
+  size_t bytes = 5 * c->fstride * sizeof(float);   // R_u, R_v, R_w, theta_rho, pi'_s
   if (bytes > (size_t)max_window) bytes = (size_t)max_window;
   size_t setaside = bytes < (size_t)max_persist ? bytes : (size_t)max_persist;
   size_t cur = 0;
@@ -390,6 +443,8 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
   if (cfg->cor_opt < 0 || cfg->cor_opt > 2) return fail(LEXGB_ERR_ARG, "cor_opt must be 0, 1 or 2");
   if (!(cfg->cs >= 0.0)) return fail(LEXGB_ERR_ARG, "cs must be >= 0 (0: the default 0.18)");
   if (cfg->acoustic_pairs != 0 && cfg->acoustic_pairs != 1) return fail(LEXGB_ERR_ARG, "acoustic_pairs must be 0 or 1");
+  if (cfg->acoustic_kernel < LEXGB_ACOUSTIC_AUTO || cfg->acoustic_kernel > LEXGB_ACOUSTIC_PERSISTENT)
+    return fail(LEXGB_ERR_ARG, "acoustic_kernel must be LEXGB_ACOUSTIC_AUTO, _ROWS, _TILE or _PERSISTENT");
   lexgb_ctx* c = new lexgb_ctx();
   c->cfg = *cfg;
   c->d = Dims{cfg->nx, cfg->ny, cfg->nz};
@@ -454,9 +509,45 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("Cs gradient: ") + cudaGetErrorString(e));
   e = cudaMemsetAsync(c->cs_bar, 0, sizeof(double), c->stream);
   if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("Cs gradient: ") + cudaGetErrorString(e));
+  e = cudaMalloc(&c->sync, 2 * sizeof(unsigned));
+  if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("barrier word: ") + cudaGetErrorString(e));
+  e = cudaMemsetAsync(c->sync, 0, 2 * sizeof(unsigned), c->stream);
+  if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e));
   e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
   if (cfg->l2_persist == 0) setup_l2_window(c);
+  if (cfg->acoustic_kernel == LEXGB_ACOUSTIC_PERSISTENT) {
+    // the persistent acoustic kernel where the grid fits it; a probe launch with no sub-step (it copies
+    // a scratch tile onto itself) checks that cooperative launches are available in this process
+    c->persist_blocks = acoustic_persist_blocks(c->d);
+    if (c->persist_blocks > 0) {
+      PersistIO io{};
+      for (int b = 0; b < 4; ++b) {
+        io.u[b] = c->Xu;
+        io.v[b] = c->Xv;
+        io.w[b] = c->Xw;
+      }
+      io.p0 = c->Xp; io.po = c->Xp;
+      io.Ru = c->Ru; io.Rv = c->Rv; io.Rw = c->Rw; io.trho = c->trho; io.ps = c->Xp;
+      io.hb[0] = io.hb[1] = c->Yp;
+      io.bar = c->sync;
+      io.status = reinterpret_cast<int*>(c->sync + 1);
+      io.spin_limit = c->spin_limit;
+      io.nsub = 0;
+      io.dtau = 0.f;
+      e = launch_acoustic_persist(c->d, c->ph, c->cols, io, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        c->persist_blocks = 0;   // one launch per sub-step instead
+      }
+    }
+  }
+  // AUTO is the rows form: measured on GB300 it is the fastest at every grid tried (192x192x96: 33.0 us
+  // per sub-step against 41.8 us tiled and 49 us persistent; 32^3 to 128x128x64 likewise)
+  c->ak = c->persist_blocks > 0 ? LEXGB_ACOUSTIC_PERSISTENT
+          : (cfg->acoustic_kernel == LEXGB_ACOUSTIC_TILE && acoustic_tile_fits(c->d)) ? LEXGB_ACOUSTIC_TILE
+                                                                                       : LEXGB_ACOUSTIC_ROWS;
   *out = c;
   return LEXGB_OK;
 }
@@ -467,6 +558,7 @@ int lexgb_destroy(lexgb_ctx* c) {
   drop_graph(c);
   if (c->l2on) cudaCtxResetPersistingL2Cache();  // return the persisting lines to normal use
   cudaFree(c->arena);
+  cudaFree(c->sync);
   cudaFree(c->rec_arena);
   cudaFree(c->adj_arena);
   cudaFree(c->sgs_arena);
@@ -561,7 +653,7 @@ int lexgb_download_state(lexgb_ctx* c, void* const fields[6], int dtype) {
     CK(cudaMemcpyAsync(fields[f], src, padded_count(c->d, kind_of(f)) * esz, cudaMemcpyDeviceToHost, c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));
-  return LEXGB_OK;
+  return take_status(c);
 }
 
 int lexgb_step(lexgb_ctx* c, int nsteps, int use_graph) {
@@ -830,12 +922,26 @@ int lexgb_check_finite(lexgb_ctx* c, long long* n_bad) {
   CK(cudaMemcpyAsync(&h, c->count, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   *n_bad = (long long)h;
-  return LEXGB_OK;
+  return take_status(c);
 }
 
 int lexgb_synchronize(lexgb_ctx* c) {
   if (!c) return fail(LEXGB_ERR_ARG, "null context");
   CK(cudaStreamSynchronize(c->stream));
+  return take_status(c);
+}
+
+int lexgb_acoustic_kernel(lexgb_ctx* c, int* kind) {
+  if (!c || !kind) return fail(LEXGB_ERR_ARG, "null argument");
+  *kind = c->ak;
+  return LEXGB_OK;
+}
+
+int lexgb_set_barrier_limit(lexgb_ctx* c, long long polls) {
+  if (!c) return fail(LEXGB_ERR_ARG, "null context");
+  c->barrier_test = polls < 0;
+  c->spin_limit = polls == 0 ? (1LL << 24) : (polls < 0 ? -polls : polls);
+  drop_graph(c);   // the limit is a kernel argument captured in the step graph
   return LEXGB_OK;
 }
 
@@ -869,6 +975,8 @@ int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
   if (which < 0 || which >= LEXGB_KERNEL_COUNT) return fail(LEXGB_ERR_ARG, "unknown kernel");
   const Dims& d = c->d;
   const StagePlan p = plan_of(c->cfg);
+  if (which == LEXGB_KERNEL_ACOUSTIC_STAGE && (c->persist_blocks == 0 || p.n[2] < 2))
+    return fail(LEXGB_ERR_STATE, "the persistent acoustic kernel is not used for this grid or configuration");
   const State& x = c->A;
   // inputs that the timed kernels read: slow tendencies of the current state
   CK(launch_div_trho(d, c->ph, c->cols, x, c->div, c->trho, c->stream));
@@ -881,7 +989,7 @@ int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
     switch (which) {
       case LEXGB_KERNEL_ACOUSTIC: {
         const AcousticOut o = (r & 1) ? Y : X;
-        cudaError_t e = launch_acoustic(d, c->ph, c->cols, in, o, (float)p.dtau[2], c->stream, r & 1);
+        cudaError_t e = sub_step(c, in, o, (float)p.dtau[2], r & 1, nullptr);
         in.u = o.u; in.v = o.v; in.w = o.w; in.p = o.p;
         return e;
       }
@@ -890,6 +998,21 @@ int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
         cudaError_t e = launch_acoustic_pair(d, c->ph, c->cols, in, o, (float)p.dtau[2], c->stream);
         in.u = o.u; in.v = o.v; in.w = o.w; in.p = o.p;
         return e;
+      }
+      case LEXGB_KERNEL_ACOUSTIC_STAGE: {   // stage 2's sub-steps from the state into scratch state C
+        PersistIO io{};
+        io.u[0] = x.u; io.u[1] = c->Xu; io.u[2] = c->Yu; io.u[3] = c->C.u;
+        io.v[0] = x.v; io.v[1] = c->Xv; io.v[2] = c->Yv; io.v[3] = c->C.v;
+        io.w[0] = x.w; io.w[1] = c->Xw; io.w[2] = c->Yw; io.w[3] = c->C.w;
+        io.p0 = x.p; io.po = c->C.p;
+        io.Ru = c->Ru; io.Rv = c->Rv; io.Rw = c->Rw; io.trho = c->trho; io.ps = x.p;
+        io.hb[0] = c->Xp; io.hb[1] = c->Yp;
+        io.bar = c->sync;
+        io.status = reinterpret_cast<int*>(c->sync + 1);
+        io.spin_limit = c->spin_limit;
+        io.nsub = p.n[2];
+        io.dtau = (float)p.dtau[2];
+        return launch_acoustic_persist(d, c->ph, c->cols, io, c->stream, c->l2on ? &c->l2win : nullptr);
       }
       case LEXGB_KERNEL_DIV_TRHO: return launch_div_trho(d, c->ph, c->cols, x, c->div, c->trho, c->stream);
       case LEXGB_KERNEL_ADV_SCALARS:
@@ -923,7 +1046,7 @@ int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   *ms_per_launch = ms / reps;
-  return LEXGB_OK;
+  return take_status(c);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -962,6 +1085,7 @@ int lexgb_get_state_interior(lexgb_ctx* c, float* fields[6], int on_device) {
     CK(cudaStreamSynchronize(c->stream));
     const size_t n = (size_t)c->d.cells();
     for (size_t t = 0; t < n; ++t) fields[0][t] += (float)c->theta_ref;
+    return take_status(c);
   }
   return LEXGB_OK;
 }
@@ -1096,7 +1220,7 @@ int adj_forward(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages) {
     AcousticIn in{A.u, A.v, A.w, A.p, w.Ru[s], w.Rv[s], w.Rw[s], w.trho[s], xs.p};
     for (int m = 1; m <= p.n[s]; ++m) {
       const AcousticOut o{w.ac[s][m][0], w.ac[s][m][1], w.ac[s][m][2], w.ac[s][m][3]};
-      CK(launch_acoustic(d, c->ph, c->cols, in, o, (float)p.dtau[s], c->stream));
+      CK(sub_step(c, in, o, (float)p.dtau[s], 0, nullptr));
       in.u = o.u; in.v = o.v; in.w = o.w; in.p = o.p;
     }
   }

@@ -290,6 +290,36 @@ cudaError_t launch_acoustic(const Dims&, const Phys&, const Cols&, AcousticIn in
 cudaError_t launch_acoustic_pair(const Dims&, const Phys&, const Cols&, AcousticIn in, AcousticOut out, float dtau,
                                  cudaStream_t);
 cudaError_t init_acoustic_attributes();
+// All sub-steps of one stage in one cooperative launch (nsub >= 2): each block keeps its tile of pi'
+// in shared memory; u, v and w of sub-step s are read from u[src] and written to u[dst] with
+// src = 0 (the stage's input winds, read only) for s = 0, else 1 + ((s-1) & 1), and dst = 3 (the
+// stage's output winds) for the last sub-step, else 1 + (s & 1); hb[0]/hb[1] (field-sized) carry the
+// tiles' edge pi' between sub-steps.  The stage's input winds and pi' may alias its outputs.
+// bar: one word, zeroed by the launcher; status: the context's sticky status word
+// (LEXGB_ERR_TIMEOUT when a bounded wait gave up after spin_limit polls).
+struct PersistIO {
+  float *u[4], *v[4], *w[4];
+  const float* p0;
+  float* po;
+  const float *Ru, *Rv, *Rw, *trho, *ps;
+  float* hb[2];
+  unsigned* bar;
+  int* status;
+  long long spin_limit;
+  int unreachable;   // test mode: every grid-barrier wait expects one arrival too many and gives up
+  int nsub;
+  float dtau;
+};
+// one sub-step on 32 x 4 x 8 blocks sharing values between warps (needs nx % 32 == 0, ny % 4 == 0);
+// same results as launch_acoustic
+bool acoustic_tile_fits(const Dims&);
+cudaError_t launch_acoustic_tile(const Dims&, const Phys&, const Cols&, AcousticIn in, AcousticOut out, float dtau,
+                                 cudaStream_t, int rev = 0, const cudaAccessPolicyWindow* win = nullptr);
+// blocks of the persistent kernel for this grid, or 0 when the grid does not fit it
+int acoustic_persist_blocks(const Dims&);
+size_t acoustic_persist_smem(const Dims&);
+cudaError_t launch_acoustic_persist(const Dims&, const Phys&, const Cols&, const PersistIO&, cudaStream_t,
+                                    const cudaAccessPolicyWindow* win = nullptr);
 // diagnostics of the acoustic operators on one state
 cudaError_t launch_diag_pgf(const Dims&, const Phys&, const Cols&, const float* p, const float* trho, float* pu,
                             float* pv, float* pw, cudaStream_t);

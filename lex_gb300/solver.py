@@ -36,11 +36,14 @@ class Solver:
     theta_ref is the constant subtracted from theta on the device (0: theta0 at level 1).
     acoustic_pairs: advance two acoustic sub-steps per kernel launch (temporal blocking).
     l2_persist: keep the acoustic sub-steps' per-stage inputs in a persisting L2 window.
+    acoustic_kernel: "auto" (the fastest measured form for the grid), "rows" or "tile" (one kernel
+    launch per sub-step) or "persistent" (one cooperative launch per stage); a form the grid does not
+    allow falls back to "auto" (see ``acoustic_form``).
     cs: the Smagorinsky constant (None: 0.18, turbulence.py:433).
     """
 
     def __init__(self, nx, ny, nz, dx, dy, dz, dt, n_sound=32, turb_opt=1, cor_opt=0, f_cor=1.0e-4,
-                 theta_ref=0.0, acoustic_pairs=False, l2_persist=True, cs=None):
+                 theta_ref=0.0, acoustic_pairs=False, l2_persist=True, cs=None, acoustic_kernel="auto"):
         self.lib = _lib.load()
         cfg = Config()
         check(self.lib.lexgb_default_config(ctypes.byref(cfg)))
@@ -51,6 +54,9 @@ class Solver:
         cfg.acoustic_pairs = 1 if acoustic_pairs else 0
         cfg.l2_persist = 0 if l2_persist else -1
         cfg.cs = float(cs) if cs is not None else 0.0
+        if acoustic_kernel not in _lib.ACOUSTIC_KERNELS:
+            raise ValueError("acoustic_kernel must be one of %s" % sorted(_lib.ACOUSTIC_KERNELS))
+        cfg.acoustic_kernel = _lib.ACOUSTIC_KERNELS[acoustic_kernel]
         self.cs = float(cs) if cs is not None else 0.18
         self.cfg = cfg
         self.nx, self.ny, self.nz = nx, ny, nz
@@ -158,6 +164,7 @@ class Solver:
         """Smagorinsky constant for the following steps."""
         check(self.lib.lexgb_set_cs(self.handle, float(cs)))
         self.cs = float(cs)
+        self._kept_token = None   # the library discards a kept step when Cs changes
 
     def cs_grad(self, reset=True):
         """d(seed . output)/dCs accumulated by the reverse-mode calls since the last reset."""
@@ -178,7 +185,21 @@ class Solver:
         return tuple(f), tuple(t)
 
     def synchronize(self):
+        """Wait for the solver's stream; raises LexError(LEXGB_ERR_TIMEOUT) when a bounded device-side
+        wait gave up since the last check (the state must then be uploaded again)."""
         check(self.lib.lexgb_synchronize(self.handle))
+
+    @property
+    def acoustic_form(self):
+        """The acoustic form this solver runs: "rows", "tile" or "persistent"."""
+        k = ctypes.c_int()
+        check(self.lib.lexgb_acoustic_kernel(self.handle, ctypes.byref(k)))
+        return {v: n for n, v in _lib.ACOUSTIC_KERNELS.items()}[k.value]
+
+    def set_barrier_limit(self, polls):
+        """Polls a grid-barrier wait of the persistent acoustic kernel makes before it gives up (0: default;
+        negative: test mode, every wait expects an arrival that never comes and gives up after -polls)."""
+        check(self.lib.lexgb_set_barrier_limit(self.handle, int(polls)))
 
     # -------------------------------------------------------------------------------- reverse mode
     def step_vjp(self, ybar, nstages=3):
@@ -228,7 +249,7 @@ class Solver:
 
     # -------------------------------------------------------------------------------- checkpoints
     _CFG = ("nx", "ny", "nz", "dx", "dy", "dz", "dt", "n_sound", "turb_opt", "cor_opt", "f_cor", "theta_ref",
-            "acoustic_pairs", "l2_persist")
+            "acoustic_pairs", "l2_persist", "acoustic_kernel")
 
     def save(self, path):
         """Checkpoint to an .npz archive: the configuration, the Smagorinsky constant, the base
@@ -248,11 +269,12 @@ class Solver:
     def restore(cls, path):
         """A new solver from a checkpoint written by save()."""
         with np.load(path) as z:
-            c = {k: z["cfg_" + k].item() for k in cls._CFG}
+            c = {k: z["cfg_" + k].item() for k in cls._CFG if "cfg_" + k in z.files}
             S = cls(int(c["nx"]), int(c["ny"]), int(c["nz"]), c["dx"], c["dy"], c["dz"], c["dt"], int(c["n_sound"]),
                     turb_opt=int(c["turb_opt"]), cor_opt=int(c["cor_opt"]), f_cor=c["f_cor"],
                     theta_ref=c["theta_ref"], acoustic_pairs=bool(c["acoustic_pairs"]),
-                    l2_persist=int(c["l2_persist"]) == 0, cs=z["cfg_cs"].item())
+                    l2_persist=int(c["l2_persist"]) == 0, cs=z["cfg_cs"].item(),
+                    acoustic_kernel={v: n for n, v in _lib.ACOUSTIC_KERNELS.items()}[int(c.get("acoustic_kernel", 0))])
             S.set_base_columns(*[z["base_" + n] for n in ("theta0", "qv0", "pi0", "rho0")])
             S.upload(tuple(z["state_" + f] for f in FIELDS))
         return S

@@ -96,6 +96,12 @@ def _unavailable(*_a, **_k):
     raise NotImplementedError("not provided by the torch stand-in")
 
 
+def set_dtype(dtype):
+    """Switch the working dtype of an installed stand-in (the imported reference modules follow)."""
+    _STATE["dtype"] = dtype
+    torch.set_default_dtype(dtype)
+
+
 def install(dtype=torch.float64):
     """Register the stand-in modules in ``sys.modules`` and set the working dtype."""
     _STATE["dtype"] = dtype

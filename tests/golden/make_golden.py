@@ -296,6 +296,9 @@ def case_bubble192_step(R, out):
              "pip": (slice(3, -3), slice(3, -3), slice(1, -1)), "qv": (slice(3, -3), slice(3, -3), slice(1, -1))}
     for s, (xi, tt) in enumerate(((xi1, t1), (xi2, t2), (xi3, t3))):
         for k, a in zip(tnames, tt):
+            a = np.asarray(a)
+            if a.shape[1] >= g["ny"] + 6:       # u, v, w and pi' tendencies come padded
+                a = a[3:-3, 3:-3, 1:-1]
             reduce_into(d, "stage%d_%s" % (s, k), a)
         for k, a in zip(FIELDS, xi):
             a = np.asarray(a)[inner[k]]
@@ -355,7 +358,9 @@ def case_bubble192_600s(R, jt, out, checkpoint=None, nsteps=600):
 def case_adjoint(R, jt, out):
     """torch.autograd through the reference's ws_rk3_big_step (torch stand-in, FP64) as the stand-in for
     jax.vjp: on the ops_random state (16 x 12 x 8, Smagorinsky on), the adjoint of the interior state for
-    seeded output seeds, after one big step and after a three-step rollout, with cor_opt 0 and 1.
+    seeded output seeds, after one big step and after a three-step rollout, with cor_opt 0 and 1.  The
+    same reverse mode run in FP32 is compared with it too: ``..._fp32err_<field>`` is the relative L2
+    difference of the reference's own FP32 adjoint from its FP64 adjoint (w on faces 1..nz-1).
 
     Inputs and outputs are in the device layout of the library (interior only, x fastest: [z][y][x],
     u and v without the duplicated periodic face, w on the nz+1 faces): the padding the reference applies
@@ -398,19 +403,29 @@ def case_adjoint(R, jt, out):
         d["x_" + k] = x.numpy()
     for k, y in zip(FIELDS, ybar):
         d["ybar_" + k] = y.numpy()
+    def vjp(cor, nsteps, dtype):
+        jt.set_dtype(dtype)
+        b, g_ = jt.tree(base), jt.tree(grids)
+        xs = [x.to(dtype).clone().requires_grad_(True) for x in x0]
+        st = tuple(from_dev(k, x) for k, x in zip(FIELDS, xs))
+        for _ in range(nsteps):
+            st, _ = R.sp.ws_rk3_big_step(st, b, g_, (2, False, False, cor, False, False, 1))
+        y = [to_dev(k, a) for k, a in zip(FIELDS, st)]
+        dot = sum((a * yb.to(dtype)).sum() for a, yb in zip(y, ybar))
+        return y, torch.autograd.grad(dot, xs)
+
     for cor in (0, 1):
-        mo = (2, False, False, cor, False, False, 1)
         for nsteps in (1, 3):
-            xs = [x.clone().requires_grad_(True) for x in x0]
-            st = tuple(from_dev(k, x) for k, x in zip(FIELDS, xs))
-            for _ in range(nsteps):
-                st, _ = R.sp.ws_rk3_big_step(st, bt, gt, mo)
-            y = [to_dev(k, a) for k, a in zip(FIELDS, st)]
-            dot = sum((a * b).sum() for a, b in zip(y, ybar))
-            gr = torch.autograd.grad(dot, xs)
-            for k, a, gg in zip(FIELDS, y, gr):
+            y, gr = vjp(cor, nsteps, torch.float64)
+            _, g32 = vjp(cor, nsteps, torch.float32)
+            for k, a, gg, g4 in zip(FIELDS, y, gr, g32):
                 d["cor%d_n%d_y_%s" % (cor, nsteps, k)] = a.detach().numpy()
                 d["cor%d_n%d_xbar_%s" % (cor, nsteps, k)] = gg.numpy()
+                ref, got = gg.numpy(), g4.double().numpy()
+                if k == "w":
+                    ref, got = ref[1:-1], got[1:-1]
+                d["cor%d_n%d_fp32err_%s" % (cor, nsteps, k)] = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    jt.set_dtype(torch.float64)
     np.savez_compressed(out, **{k: np.asarray(v) for k, v in d.items()})
 
 

@@ -28,7 +28,7 @@ def report():
         json.dump(REPORT, f, indent=1, sort_keys=True)
 
 
-def _setup(nstages, turb=0):
+def _setup(nstages, turb=0, cor=0):
     from oracle.ic import Grid
     from oracle.dycore import Dycore
     from lex_gb300.solver import Solver
@@ -36,9 +36,9 @@ def _setup(nstages, turb=0):
     nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
     base = dict(theta0=g["col_theta0"], qv0=g["col_qv0"], pi0=g["col_pi0"], rho0=g["col_rho0"])
     D = Dycore(Grid(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"])), base, float(g["dt"]),
-               int(g["n_sound"]), turb=bool(turb))
+               int(g["n_sound"]), turb=bool(turb), cor_opt=cor)
     S = Solver(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"]), float(g["dt"]), int(g["n_sound"]),
-               turb_opt=turb)
+               turb_opt=turb, cor_opt=cor)
     S.set_base_columns(g["col_theta0"], g["col_qv0"], g["col_pi0"], g["col_rho0"])
     x0 = tuple(g["in_" + f] for f in FIELDS)
     S.upload(x0)
@@ -75,15 +75,16 @@ def _direction(rng, nx, ny, nz):
             w, rng.standard_normal((nx, ny, nz)) * 1e-4, rng.standard_normal((nx, ny, nz)) * 1e-4)
 
 
-CASES = [(1, None, 0), (1, "theta", 0), (1, "pip", 0), (1, "u", 0), (1, "w", 0), (3, None, 0),
-         (1, None, 1), (1, "theta", 1), (1, "u", 1), (1, "w", 1), (3, None, 1)]
+CASES = [(1, None, 0, 0), (1, "theta", 0, 0), (1, "pip", 0, 0), (1, "u", 0, 0), (1, "w", 0, 0), (3, None, 0, 0),
+         (1, None, 1, 0), (1, "theta", 1, 0), (1, "u", 1, 0), (1, "w", 1, 0), (3, None, 1, 0),
+         (3, None, 1, 1), (3, "v", 1, 2)]
 
 
-@pytest.mark.parametrize("nstages,only,turb", CASES,
-                         ids=["%s%s%s" % ("step" if n == 3 else "stage0", "_" + o if o else "", "_smag" if t else "")
-                              for n, o, t in CASES])
-def test_reverse_mode_matches_oracle_finite_differences(built_lib, nstages, only, turb):
-    g, D, S, x0, forward = _setup(nstages, turb)
+@pytest.mark.parametrize("nstages,only,turb,cor", CASES,
+                         ids=["%s%s%s%s" % ("step" if n == 3 else "stage0", "_" + o if o else "", "_smag" if t else "",
+                                            "_cor%d" % c if c else "") for n, o, t, c in CASES])
+def test_reverse_mode_matches_oracle_finite_differences(built_lib, nstages, only, turb, cor):
+    g, D, S, x0, forward = _setup(nstages, turb, cor)
     nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
     rng = np.random.default_rng(7)
     errs = []
@@ -103,7 +104,7 @@ def test_reverse_mode_matches_oracle_finite_differences(built_lib, nstages, only
         scale = np.sqrt(sum(float(np.sum(a * a)) for a in yb)) * np.sqrt(sum(float(np.sum(a * a)) for a in jv))
         errs.append((lhs, rhs, abs(lhs - rhs) / scale))
     S.close()
-    REPORT["%d_%s_%d" % (nstages, only, turb)] = errs
+    REPORT["%d_%s_%d_cor%d" % (nstages, only, turb, cor)] = errs
     assert all(e[2] <= TOL for e in errs), errs
 
 
@@ -131,3 +132,38 @@ def test_kept_step_reverse_equals_recomputed_reverse(built_lib):
         np.testing.assert_array_equal(a, b)
     for a, b in zip(out, ref):
         np.testing.assert_array_equal(a.transpose(2, 1, 0), b)
+
+
+@pytest.mark.parametrize("cor,nsteps", [(0, 1), (0, 3), (1, 1), (1, 3)],
+                         ids=["step", "rollout3", "step_coriolis", "rollout3_coriolis"])
+def test_reverse_mode_matches_reference_autograd(built_lib, cor, nsteps):
+    """The library's reverse mode against the reference's own: torch.autograd through the reference's
+    unmodified ws_rk3_big_step (one_sprint_functions.py:10-30) under the torch stand-in for jax, FP64,
+    Smagorinsky on (tests/golden/adjoint_vjp.npz, the stand-in for jax.vjp of the reference step).
+    One big step and a three-step rollout through lex_gb300.autograd (step-level checkpointing), with
+    and without Coriolis.  Bar, per field (relative L2 against the FP64 adjoint; w on faces 1..nz-1,
+    which are the state's free values): within 1e-5, or no further from it than the reference's own
+    reverse mode run in FP32 is (stored in the fixture), whichever is larger."""
+    import torch
+    from lex_gb300 import autograd as lag
+    from lex_gb300.solver import Solver
+    g = load_golden("adjoint_vjp.npz")
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    S = Solver(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"]), float(g["dt"]), int(g["n_sound"]),
+               turb_opt=1, cor_opt=cor, f_cor=float(g["f_cor"]))
+    S.set_base_columns(g["col_theta0"], g["col_qv0"], g["col_pi0"], g["col_rho0"])
+    x = [torch.tensor(g["x_" + f], dtype=torch.float32, device="cuda").requires_grad_(True) for f in FIELDS]
+    y = lag.rollout(S, tuple(x), nsteps)
+    yb = [torch.tensor(g["ybar_" + f], dtype=torch.float32, device="cuda") for f in FIELDS]
+    gx = torch.autograd.grad(y, x, yb)
+    S.close()
+    errs, bars = {}, {}
+    for f, a in zip(FIELDS, gx):
+        ref = g["cor%d_n%d_xbar_%s" % (cor, nsteps, f)]
+        got = a.double().cpu().numpy()
+        if f == "w":
+            ref, got = ref[1:-1], got[1:-1]
+        errs[f] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        bars[f] = max(1e-5, float(g["cor%d_n%d_fp32err_%s" % (cor, nsteps, f)]))
+    REPORT["reference_autograd_cor%d_n%d" % (cor, nsteps)] = {"err": errs, "bar": bars}
+    assert all(errs[f] <= bars[f] for f in FIELDS), (errs, bars)

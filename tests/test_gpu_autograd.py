@@ -108,3 +108,31 @@ def test_rollout_gradient_with_respect_to_cs(built_lib):
     scale = np.sqrt(sum(float(np.sum(a * a)) for a in yb)) * np.sqrt(sum(float(np.sum(a * a)) for a in jv))
     assert abs(lhs) > 1e-3 * scale                     # Cs matters in this case
     assert abs(lhs - got) <= 1e-4 * scale, (lhs, got, scale)
+
+
+def test_backward_uses_the_cs_of_its_forward(built_lib):
+    """A step's backward differentiates the step with the Cs its forward used, even when the solver's
+    Cs is changed before backward (the forward's Cs is recorded and restored around the reverse pass)."""
+    torch = pytest.importorskip("torch")
+    from lex_gb300.solver import Solver
+    from lex_gb300 import autograd as lag
+    g = load_golden("ops_random.npz")
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    x0 = tuple(g["in_" + f] for f in FIELDS)
+    yb = _direction(np.random.default_rng(5), nx, ny, nz)
+    grads = []
+    with Solver(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"]), float(g["dt"]), int(g["n_sound"]),
+                turb_opt=1) as S:
+        S.set_base_columns(g["col_theta0"], g["col_qv0"], g["col_pi0"], g["col_rho0"])
+        for change in (False, True):
+            S.set_cs(0.18)
+            state = tuple(_to_dev(a).requires_grad_(True) for a in _interior(x0, nx, ny))
+            out = lag.rollout(S, state, 2)
+            if change:
+                S.set_cs(0.3)
+            loss = sum((o * _to_dev(y)).sum() for o, y in zip(out, yb))
+            loss.backward()
+            grads.append([_from_dev(t.grad) for t in state])
+            assert S.cs == (0.3 if change else 0.18)      # restored after the reverse pass
+    for a, b in zip(*grads):
+        np.testing.assert_array_equal(a, b)

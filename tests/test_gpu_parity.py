@@ -217,3 +217,34 @@ def test_warm_bubble_600s_32cube(built_lib):
         REPORT["bubble600s_" + k] = e
     # FP32 after 200 steps of a developing thermal: theta' and qv' within 1e-3, w within 2e-3
     assert errs["theta_p"] < 1e-3 and errs["qv_p"] < 1e-3 and errs["w"] < 2e-3, errs
+
+
+@pytest.mark.parametrize("cor", [1, 2], ids=["coriolis", "coriolis_lspgrad"])
+def test_coriolis_stages_match_reference(built_lib, cor):
+    """cor_opt 1 and 2 (calculate_coriolis_force / _with_lspgrad, pressure_gradient_coriolis.py:80-113,
+    added to R_u and R_v at one_step_integration.py:127-132): every stage tendency within 1e-5 of the
+    reference's (tests/golden/ops_coriolis.npz) and the step within 1e-5 of its increment."""
+    from conftest import load_golden
+    from lex_gb300.solver import Solver
+    g = load_golden("ops_coriolis.npz")
+    x0 = tuple(g["in_" + f] for f in FIELDS)
+    with Solver(int(g["nx"]), int(g["ny"]), int(g["nz"]), float(g["dx"]), float(g["dy"]), float(g["dz"]),
+                float(g["dt"]), int(g["n_sound"]), turb_opt=1, cor_opt=cor, f_cor=float(g["f_cor"])) as S:
+        S.set_base_columns(g["col_theta0"], g["col_qv0"], g["col_pi0"], g["col_rho0"])
+        S.upload(x0)
+        S.step_record()
+        for s in range(3):
+            _, tends = S.stage(s)
+            for n, a in zip(("dtheta", "du", "dv", "dw", "dpip", "dqv"), tends):
+                ref = g["cor%d_stage%d_%s" % (cor, s, n)]
+                if ref.shape != a.shape:
+                    ref = inner(ref)
+                err = rel_l2(a, ref)
+                REPORT["cor%d_stage%d_%s" % (cor, s, n)] = err
+                assert err <= 1e-5, (cor, s, n, err)
+        S.upload(x0)
+        S.step(1)
+        for f, a, a0 in zip(FIELDS, S.download(), x0):
+            err = state_err(a, g["cor%d_step_%s" % (cor, f)], a0, f)
+            REPORT["cor%d_step_%s" % (cor, f)] = err
+            assert err <= 1e-5, (cor, f, err)
