@@ -202,13 +202,9 @@ int run_stage(lexgb_ctx* c, int s, const State& xi0, const State& xis, const Sta
   // acoustic_pairs, sub-steps go two per launch (an odd count starts with a single one).
   const int n = p.n[s];
   const float dtau = (float)p.dtau[s];
-  // pi'_s joins the persisting window (R_u, R_v, R_w, theta_rho, then this slot): the divergence
-  // field after theta_rho is free once the advection kernels above have read it
+  // (pi'_s stays outside the persisting window: a fifth field there, 71 MB at 192x192x96, measured
+  // 2.74 ms per step against 2.70 ms with four, the set-aside crowding out the moving state)
   const float* ps = xis.p;
-  if (c->l2on && c->l2win.num_bytes >= 5 * c->fstride * sizeof(float) && n > 1) {
-    CK(cudaMemcpyAsync(c->div, xis.p, (size_t)c->d.cells() * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
-    ps = c->div;
-  }
   AcousticIn in{xi0.u, xi0.v, xi0.w, xi0.p, c->Ru, c->Rv, c->Rw, c->trho, ps};
   const AcousticOut X{c->Xu, c->Xv, c->Xw, c->Xp}, Y{c->Yu, c->Yv, c->Yw, c->Yp};
   const AcousticOut O{out.u, out.v, out.w, out.p};
@@ -379,11 +375,10 @@ int build_table(lexgb_ctx* c) {
 
 extern "C" {
 
-// The acoustic sub-steps of a stage all read R_u, R_v, R_w, theta_rho and pi'_s (five adjacent arena
-// fields, pi'_s copied into the slot after theta_rho for the stage): a persisting L2 window over
-// them (up to the device's set-aside maximum) keeps them on chip across the 16 or 32 sub-steps, so
-// only the moving state streams through HBM.  The set-aside is a limit of this process's context;
-// failures leave normal caching.
+// The acoustic sub-steps of a stage all read R_u, R_v, R_w and theta_rho (four adjacent arena
+// fields): a persisting L2 window over them (up to the device's set-aside maximum) keeps them
+// on chip across the 16 or 32 sub-steps, so only the moving state streams through HBM.  The
+// set-aside is a limit of this process's context; failures leave normal caching.
 static void setup_l2_window(lexgb_ctx* c) {
   int dev = 0, max_persist = 0, max_window = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -393,7 +388,7 @@ static void setup_l2_window(lexgb_ctx* c) {
     cudaGetLastError();
     return;
   }
-  size_t bytes = 5 * c->fstride * sizeof(float);   // R_u, R_v, R_w, theta_rho, pi'_s
+  size_t bytes = 4 * c->fstride * sizeof(float);   // R_u, R_v, R_w, theta_rho
   if (bytes > (size_t)max_window) bytes = (size_t)max_window;
   size_t setaside = bytes < (size_t)max_persist ? bytes : (size_t)max_persist;
   size_t cur = 0;
