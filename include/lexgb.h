@@ -266,21 +266,23 @@ int lexgb_cnn_adam(long long n, float *w, const float *gw, float *m, float *v, v
                    float beta2, float eps, int step, void *stream);
 
 /* Learned SGS correction fused into lexgb_step: after every big step the CNN corrects theta, u,
- * v, w and qv (pi' is not corrected), as ws_rk3_sprint_dl does (one_sprint_functions.py:118-163):
- *   input  x_f = (field_f - in_lo[f][k]) / in_range[f][k]   (theta in K; u, v, w averaged to the
- *            cell centre; f = theta, u, v, w, qv; k the level)          (dl_models.py:125-155)
+ * v, w and qv (pi' is not corrected) the way ws_rk3_sprint_dl does (one_sprint_functions.py:118-163):
+ *   input  x_f = (value - in_lo[f][l]) / in_range[f][l] on each field's own points (theta in K; l the
+ *            level, for w the face level 0..nz), then u, v, w averaged to the cell centre
+ *                                                                  (phys_state_tuple2array, dl_models.py:125-155)
  *   output c = CNN(x) (16 -> 32 -> 32 -> 32 -> 8 channels, 5 used)
- *   state += c_f * out_range[f][cell], theta and qv at the cell, u (v) at a face as the mean of
- *            the two cells beside it (periodic), w at the interior faces as the mean of the cells
- *            below and above                                          (dl_models.py:158-182)
+ *   state += (c staggered) * out_range[f] at the point: theta and qv at the cell; u (v) on the west
+ *            (south) face i >= 1 the mean of the two cells beside it, on face 0 the value of face nx-1;
+ *            w on the interior faces the mean of the cells below and above    (correct_array2tuple and
+ *            stagger_uvw, dl_models.py:158-182; one_sprint_functions.py:139-151)
  * w[l]: BF16 weights [27][cout][cin] of layer l with (cin, cout) = (16,32), (32,32), (32,32),
- * (32,8) (padding rows and columns zero); b[l]: FP32 biases [cout]; in_lo, in_range: FP32 [5][nz];
- * out_range: FP32 [5][nz][ny][nx].  All device pointers, copied on the bound stream: a later call
- * replaces the weights and ranges without rebuilding the step graph.  enable = 0 turns the
- * correction off (the other arguments may be NULL).  Needs nx a multiple of 16.  Not applied by
- * lexgb_step_record, lexgb_step_keep or the reverse mode (training differentiates the correction
- * outside the library).  No counterpart function in the reference, which applies the network in
- * Python after each ws_rk3_big_step call. */
+ * (32,8) (padding rows and columns zero); b[l]: FP32 biases [cout]; in_lo, in_range: FP32 [5][nz+1]
+ * (entry nz used by w only); out_range: FP32 [5][nz+1][ny][nx] (level nz used by w's lid face only).
+ * All device pointers, copied on the bound stream: a later call replaces the weights and ranges
+ * without rebuilding the step graph.  enable = 0 turns the correction off (the other arguments may be
+ * NULL).  Needs nx a multiple of 16.  Not applied by lexgb_step_record, lexgb_step_keep or the reverse
+ * mode (training differentiates the correction outside the library).  No counterpart function in the
+ * reference, which applies the network in Python after each ws_rk3_big_step call. */
 int lexgb_set_sgs_net(lexgb_ctx *ctx, const void *const w[4], const float *const b[4], const float *in_lo,
                       const float *in_range, const float *out_range, int enable);
 

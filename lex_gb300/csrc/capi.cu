@@ -713,8 +713,9 @@ int lexgb_set_sgs_net(lexgb_ctx* c, const void* const w[4], const float* const b
     o_b[l] = off;
     off += up(SGS_COUT[l] * sizeof(float));
   }
-  const size_t o_lo = off, o_rin = (off += up(5 * d.nz * sizeof(float))), o_rout = (off += up(5 * d.nz * sizeof(float)));
-  const size_t o_corr = (off += up(5 * cells * sizeof(float)));
+  const size_t levels = (size_t)d.nz + 1, rcount = 5 * (size_t)d.plane() * levels;
+  const size_t o_lo = off, o_rin = (off += up(5 * levels * sizeof(float))), o_rout = (off += up(5 * levels * sizeof(float)));
+  const size_t o_corr = (off += up(rcount * sizeof(float)));
   const size_t o_x = (off += up(8 * cells * sizeof(float)));
   const size_t o_a0 = (off += up(cells * 16 * 2));
   const size_t o_a1 = (off += up(cells * 32 * 2));
@@ -742,9 +743,9 @@ int lexgb_set_sgs_net(lexgb_ctx* c, const void* const w[4], const float* const b
     CK(cudaMemcpyAsync(c->sgs_w[l], w[l], wbytes[l], cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaMemcpyAsync(c->sgs_b[l], b[l], SGS_COUT[l] * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
   }
-  CK(cudaMemcpyAsync(c->sgs_lo, in_lo, 5 * d.nz * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
-  CK(cudaMemcpyAsync(c->sgs_rin, in_range, 5 * d.nz * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
-  CK(cudaMemcpyAsync(c->sgs_rout, out_range, 5 * cells * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->sgs_lo, in_lo, 5 * levels * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->sgs_rin, in_range, 5 * levels * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->sgs_rout, out_range, rcount * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
   CK(conv_prepare());
   if (!c->sgs_on) {
     CK(cudaStreamSynchronize(c->stream));

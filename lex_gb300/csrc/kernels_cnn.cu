@@ -18,8 +18,8 @@
 //   k_bias_grad    db[co] = sum_p g[p][co]
 //   k_adam         Adam update of FP32 master weights and their BF16 copies
 //   k_sgs_pack     the network's input from the device-layout state (dl_models.py:125-155)
-//   k_sgs_unpack   the scaled, re-staggered correction added to the state
-//                  (one_sprint_functions.py:136-151)
+//   k_sgs_unpack   the re-staggered, scaled correction added to the state
+//                  (dl_models.py:158-182, one_sprint_functions.py:136-151)
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -384,6 +384,10 @@ __global__ void k_adam(long long n, float* __restrict__ w, const float* __restri
 // with theta = T + theta_ref and the winds averaged to the cell centre (u, v periodic).  The
 // arithmetic is the element-wise sequence of the PyTorch packing of the same state, rounded
 // the same way (no contractions), so both give the same BF16 inputs.
+// Network input of one cell, as dl_models.phys_state_tuple2array makes it (dl_models.py:125-155):
+// every field is min-max normalised on its own grid points with per-level constants lo[f][l] and
+// rin[f][l] (stride nz+1: w's constants are per face level 0..nz), then the normalised winds are
+// averaged to the cell centre (unstagger_uvw).  16 BF16 channels, 5 used.
 __global__ void k_sgs_pack(int nx, int ny, int nz, const float* __restrict__ T, const float* __restrict__ u,
                            const float* __restrict__ v, const float* __restrict__ w, const float* __restrict__ q,
                            float theta_ref, const float* __restrict__ lo, const float* __restrict__ rin,
@@ -395,15 +399,17 @@ __global__ void k_sgs_pack(int nx, int ny, int nz, const float* __restrict__ T, 
   const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
   const long long tu = t - i + (i + 1 == nx ? 0 : i + 1);
   const long long tv = t + (long long)((j + 1 == ny ? 0 : j + 1) - j) * nx;
+  const int L = nz + 1;
+  auto nrm = [&](float x, int f, int l) { return __fdiv_rn(__fsub_rn(x, lo[f * L + l]), rin[f * L + l]); };
   float f[5];
-  f[0] = __fadd_rn(T[t], theta_ref);
-  f[1] = __fmul_rn(0.5f, __fadd_rn(u[t], u[tu]));
-  f[2] = __fmul_rn(0.5f, __fadd_rn(v[t], v[tv]));
-  f[3] = __fmul_rn(0.5f, __fadd_rn(w[t], w[t + plane]));
-  f[4] = q[t];
+  f[0] = nrm(__fadd_rn(T[t], theta_ref), 0, k);
+  f[1] = __fmul_rn(0.5f, __fadd_rn(nrm(u[t], 1, k), nrm(u[tu], 1, k)));
+  f[2] = __fmul_rn(0.5f, __fadd_rn(nrm(v[t], 2, k), nrm(v[tv], 2, k)));
+  f[3] = __fmul_rn(0.5f, __fadd_rn(nrm(w[t], 3, k), nrm(w[t + plane], 3, k + 1)));
+  f[4] = nrm(q[t], 4, k);
   __nv_bfloat16 h[6];
 #pragma unroll
-  for (int c = 0; c < 5; ++c) h[c] = __float2bfloat16_rn(__fdiv_rn(__fsub_rn(f[c], lo[c * nz + k]), rin[c * nz + k]));
+  for (int c = 0; c < 5; ++c) h[c] = __float2bfloat16_rn(f[c]);
   h[5] = __float2bfloat16_rn(0.f);
   uint4 a, b = make_uint4(0u, 0u, 0u, 0u);
   a.x = (uint32_t)__bfloat16_as_ushort(h[0]) | ((uint32_t)__bfloat16_as_ushort(h[1]) << 16);
@@ -414,27 +420,32 @@ __global__ void k_sgs_pack(int nx, int ny, int nz, const float* __restrict__ T, 
   x16[2 * t + 1] = b;
 }
 
-// The correction corr[p][0..4] (FP32, 8 channels a point) times the output range rout[f][p],
-// back on the grid: theta and qv at the cell, u (v) at the west (south) face as the mean of the
-// two cells beside it (periodic), w at the interior faces 1..nz-1 as the mean of the cells below
-// and above (the bottom and lid faces are not corrected).  One thread per cell; it writes only
-// its own cell and its own west, south and bottom faces.
+// The correction corr[p][0..4] (FP32, 8 channels a point) back on the grid as
+// dl_models.correct_array2tuple and one_sprint_functions.py:139-151 apply it: theta and qv at the
+// cell; u (v) on the west (south) face i >= 1 as the mean of the two cells beside it and on face 0
+// the value of face nx-1 (stagger_uvw copies the face next to the far end onto the end face,
+// dl_models.py:172-182); w on the interior faces 1..nz-1 as the mean of the cells below and above
+// (bottom and lid untouched); each times the output range at its own point, rout[f][l][j][i]
+// (stride nz+1 levels: cells for theta and qv, west / south faces for u / v, faces 0..nz for w).
+// One thread per cell; it writes only its own cell and its own west, south and bottom faces.
 __global__ void k_sgs_unpack(int nx, int ny, int nz, const float* __restrict__ corr, const float* __restrict__ rout,
                              float* __restrict__ T, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
                              float* __restrict__ q) {
   pdl_wait();
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long plane = (long long)nx * ny, cells = plane * nz;
+  const long long plane = (long long)nx * ny, cells = plane * nz, rstride = plane * (nz + 1);
   if (t >= cells) return;
   const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
-  auto c = [&](long long p, int f) { return __fmul_rn(corr[p * 8 + f], rout[f * cells + p]); };
-  const long long tu = t - i + (i == 0 ? nx - 1 : i - 1);
-  const long long tv = t + (long long)((j == 0 ? ny - 1 : j - 1) - j) * nx;
-  T[t] = __fadd_rn(T[t], c(t, 0));
-  u[t] = __fadd_rn(u[t], __fmul_rn(0.5f, __fadd_rn(c(t, 1), c(tu, 1))));
-  v[t] = __fadd_rn(v[t], __fmul_rn(0.5f, __fadd_rn(c(t, 2), c(tv, 2))));
-  if (k > 0) w[t] = __fadd_rn(w[t], __fmul_rn(0.5f, __fadd_rn(c(t - plane, 3), c(t, 3))));
-  q[t] = __fadd_rn(q[t], c(t, 4));
+  auto c = [&](long long p, int f) { return corr[p * 8 + f]; };
+  auto r = [&](long long p, int f) { return rout[f * rstride + p]; };
+  // the two cells beside the west (south) face; face 0 takes cells nx-2, nx-1 (ny-2, ny-1)
+  const long long ua = i > 0 ? t - 1 : t + (nx - 2), ub = i > 0 ? t : t + (nx - 1);
+  const long long va = j > 0 ? t - nx : t + (long long)(ny - 2) * nx, vb = j > 0 ? t : t + (long long)(ny - 1) * nx;
+  T[t] = __fadd_rn(T[t], __fmul_rn(c(t, 0), r(t, 0)));
+  u[t] = __fadd_rn(u[t], __fmul_rn(__fmul_rn(0.5f, __fadd_rn(c(ua, 1), c(ub, 1))), r(t, 1)));
+  v[t] = __fadd_rn(v[t], __fmul_rn(__fmul_rn(0.5f, __fadd_rn(c(va, 2), c(vb, 2))), r(t, 2)));
+  if (k > 0) w[t] = __fadd_rn(w[t], __fmul_rn(__fmul_rn(0.5f, __fadd_rn(c(t - plane, 3), c(t, 3))), r(t, 3)));
+  q[t] = __fadd_rn(q[t], __fmul_rn(c(t, 4), r(t, 4)));
 }
 }  // namespace
 

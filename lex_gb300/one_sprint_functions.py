@@ -120,12 +120,12 @@ def sgs_arrays(dl_params, scaling_params, nx, ny, nz):
     [cout]}} (dl_models.py:19-30, flax: cross-correlation, zero padding) -> BF16 [27][cout][cin]
     with the offset (dz+1)*9 + (dy+1)*3 + (dx+1), channels zero-padded to the kernels' widths.
     scaling_params: (theta_min, theta_max, u_min, u_max, v_min, v_max, w_min, w_max, qv_min,
-    qv_max, ...) with keepdims shapes (dataset_generation.py:80-105).  Input: per-level minimum
-    and max - min + 0.01 (1e-5 for qv) over x and y (dl_models.py:128-152); output: the per-cell
-    max - min (one_sprint_functions.py:139-143).  Where the reference's ranges live on faces
-    (u, v, w), the two faces of a cell are averaged, because the library scales the cell-centred
-    correction before staggering it.  Returns (weights [27][cout][cin] FP32 per layer, biases,
-    {'lo', 'rin': [5][nz], 'rout': [5][nz][ny][nx]})."""
+    qv_max, ...) with keepdims shapes on each field's own points (dataset_generation.py:80-105).
+    Input: per-level minimum and max - min + 0.01 (1e-5 for qv) over x and y (dl_models.py:128-152),
+    per face level for w; output: max - min at every point (one_sprint_functions.py:139-143), u and v
+    on their faces 0..nx-1 / 0..ny-1 (the duplicated periodic face nx / ny is not stored), w on faces
+    0..nz.  Returns (weights [27][cout][cin] FP32 per layer, biases, {'lo', 'rin': [5][nz+1],
+    'rout': [5][nz+1][ny][nx]}), entry / level nz repeating the top level for all but w."""
     from . import sgs_cnn
     ws, bs = [], []
     for li, (cin, cout, _) in enumerate(sgs_cnn.LAYERS):
@@ -141,21 +141,19 @@ def sgs_arrays(dl_params, scaling_params, nx, ny, nz):
         bs.append(b)
     if len(scaling_params) < 10:
         raise ValueError("scaling_params must hold (theta, u, v, w, qv) minima and maxima")
+    own = ((nx, ny, nz), (nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1), (nx, ny, nz))
     lo, rin, rout = [], [], []
     for f, margin in enumerate((0.01, 0.01, 0.01, 0.01, 1.0e-5)):
         mn = np.asarray(scaling_params[2 * f], np.float64).squeeze()
         mx = np.asarray(scaling_params[2 * f + 1], np.float64).squeeze()
+        if mn.shape != own[f] or mx.shape != own[f]:
+            raise ValueError("scaling_params[%d:%d] have shape %s, expected %s on the grid"
+                             % (2 * f, 2 * f + 2, mn.shape, own[f]))
         l, h = mn.min(axis=(0, 1)), mx.max(axis=(0, 1))
-        r = mx - mn
-        if f == 3 and l.size == nz + 1:       # w on faces
-            l, h = 0.5 * (l[:-1] + l[1:]), 0.5 * (h[:-1] + h[1:])
-            r = 0.5 * (r[:, :, :-1] + r[:, :, 1:])
-        if f == 1 and r.shape[0] == nx + 1:
-            r = 0.5 * (r[:-1] + r[1:])
-        if f == 2 and r.shape[1] == ny + 1:
-            r = 0.5 * (r[:, :-1] + r[:, 1:])
-        if l.shape != (nz,) or r.shape != (nx, ny, nz):
-            raise ValueError("scaling_params[%d:%d] do not match the grid" % (2 * f, 2 * f + 2))
+        r = (mx - mn)[:nx, :ny]                       # u, v: faces 0..nx-1 / 0..ny-1
+        if f != 3:                                    # repeat the top level as entry nz
+            l, h = np.append(l, l[-1]), np.append(h, h[-1])
+            r = np.concatenate([r, r[:, :, -1:]], axis=2)
         lo.append(l)
         rin.append(h - l + margin)
         rout.append(r.transpose(2, 1, 0))

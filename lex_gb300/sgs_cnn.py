@@ -10,17 +10,19 @@ same kernel on the mirrored, transposed weights for the input gradients, ``lexgb
 and ``lexgb_cnn_conv3d_dw`` for the weight and bias gradients.  ``adam_step`` updates the FP32
 master weights with ``lexgb_cnn_adam`` (the reference uses optax.lamb, lex_dl_train.py).
 
-Packing (dl_models.py:125-182): theta, u, v, w, qv are min-max normalised per level, the winds
-averaged to cell centres first; the correction is scaled by an output range per cell and its
-winds go back to faces by the periodic average in x and y and by averaging to interior w faces
-(zero at the bottom and the lid).  The reference normalises the staggered winds before averaging
-them and its stagger_uvw copies an interior face value to the periodic end faces; this module
-averages first and uses the periodic neighbour.  Packing runs as torch element-wise operations
-here (differentiable, for training) and as the kernels of ``lexgb_set_sgs_net`` inside the
-library's step (inference, :func:`attach`); both round the same way.
+Packing, as the reference's (dl_models.py:125-182, one_sprint_functions.py:136-151): theta, u, v, w,
+qv are min-max normalised on their own points with per-level constants (w per face level), the
+normalised winds averaged to cell centres (unstagger_uvw); the correction's winds go back to the
+faces as stagger_uvw puts them (the mean of the two cells beside a face, face 0 of u and v taking the
+value of face nx-1 / ny-1, w zero on the bottom and the lid) and every field is scaled by the output
+range at its own point.  Packing runs as torch element-wise operations here (differentiable, for
+training) and as the kernels of ``lexgb_set_sgs_net`` inside the library's step (inference,
+:func:`attach`); both round the same way.
 
-A scale is a dict of CUDA tensors: ``lo`` and ``rin`` [5, nz] (input minimum and range per
-level) and ``rout`` [5, nz, ny, nx] (output range per cell), fields (theta, u, v, w, qv).
+A scale is a dict of CUDA tensors, fields (theta, u, v, w, qv): ``lo`` and ``rin`` [5, nz+1]
+(input minimum and range per level; entry nz is used by w's lid face only, the other fields repeat
+their top level there) and ``rout`` [5, nz+1, ny, nx] (output range at each field's points: cells
+for theta and qv, west / south faces for u / v, faces 0..nz for w).
 """
 import ctypes
 
@@ -184,26 +186,33 @@ FIELDS5 = ("theta", "u", "v", "w", "qv")
 def pack(state, scale):
     """state: six CUDA tensors (nz, ny, nx) / w (nz+1, ny, nx) -> [npts, 5] normalised, x fastest."""
     th, u, v, w, _, q = state
-    ui = 0.5 * (u + torch.roll(u, -1, dims=2))
-    vi = 0.5 * (v + torch.roll(v, -1, dims=1))
-    wi = 0.5 * (w[:-1] + w[1:])
+    nz = th.shape[0]
     lo, rin = scale["lo"], scale["rin"]
-    cols = []
-    for f, a in enumerate((th, ui, vi, wi, q)):
-        cols.append(((a - lo[f].view(-1, 1, 1)) / rin[f].view(-1, 1, 1)).reshape(-1))
-    return torch.stack(cols, 1)
+    n = lambda a, f, m: (a - lo[f, :m].view(-1, 1, 1)) / rin[f, :m].view(-1, 1, 1)
+    un, vn, wn = n(u, 1, nz), n(v, 2, nz), n(w, 3, nz + 1)
+    cols = (n(th, 0, nz), 0.5 * (un + torch.roll(un, -1, dims=2)), 0.5 * (vn + torch.roll(vn, -1, dims=1)),
+            0.5 * (wn[:-1] + wn[1:]), n(q, 4, nz))
+    return torch.stack([c.reshape(-1) for c in cols], 1)
+
+
+def stagger(c, dim):
+    """Cell values -> faces as stagger_uvw puts them (dl_models.py:172-182): face i >= 1 the mean of
+    cells i-1 and i, face 0 the value of face n-1 (the face next to the far end)."""
+    s = 0.5 * (c + torch.roll(c, 1, dims=dim))
+    n = c.shape[dim]
+    return torch.cat([s.narrow(dim, n - 1, 1), s.narrow(dim, 1, n - 1)], dim)
 
 
 def unpack(corr, scale, dims):
     """[npts, 5] correction -> additions to (theta, u, v, w, pi', qv) on the staggered grid."""
     nx, ny, nz = dims
-    f = [corr[:, i].reshape(nz, ny, nx) * scale["rout"][i] for i in range(5)]
-    th, ui, vi, wi, q = f
-    u = 0.5 * (ui + torch.roll(ui, 1, dims=2))
-    v = 0.5 * (vi + torch.roll(vi, 1, dims=1))
-    z = torch.zeros(1, ny, nx, device=corr.device)
-    w = torch.cat([z, 0.5 * (wi[:-1] + wi[1:]), z], 0)
-    return (th, u, v, w, torch.zeros_like(th), q)
+    c = [corr[:, i].reshape(nz, ny, nx) for i in range(5)]
+    r = scale["rout"]
+    z = torch.zeros(1, ny, nx, device=corr.device, dtype=corr.dtype)
+    w = torch.cat([z, 0.5 * (c[3][:-1] + c[3][1:]), z], 0) * r[3]
+    th = c[0] * r[0, :nz]
+    return (th, stagger(c[1], 2) * r[1, :nz], stagger(c[2], 1) * r[2, :nz], w, torch.zeros_like(th),
+            c[4] * r[4, :nz])
 
 
 def correct(net, state, scale, dims):
@@ -212,24 +221,33 @@ def correct(net, state, scale, dims):
     return tuple(a + b for a, b in zip(state, d))
 
 
-def cell_fields(state):
-    """(theta, ui, vi, wi, qv) at cell centres: the quantities the scale's ranges describe."""
+def level_extrema(state):
+    """Per-level minima and maxima of (theta, u, v, w, qv) on their own points, [5, nz+1] each
+    (w per face level; the other fields repeat their top level in entry nz)."""
     th, u, v, w, _, q = state
-    return (th, 0.5 * (u + torch.roll(u, -1, dims=2)), 0.5 * (v + torch.roll(v, -1, dims=1)), 0.5 * (w[:-1] + w[1:]), q)
+    lo, hi = [], []
+    for a in (th, u, v, w, q):
+        mn, mx = a.amin(dim=(1, 2)), a.amax(dim=(1, 2))
+        if mn.shape[0] == th.shape[0]:
+            mn, mx = torch.cat([mn, mn[-1:]]), torch.cat([mx, mx[-1:]])
+        lo.append(mn)
+        hi.append(mx)
+    return torch.stack(lo), torch.stack(hi)
 
 
 def make_scale(states, margins=(0.01, 0.01, 0.01, 0.01, 1.0e-5)):
     """Per-level minimum and maximum over `states` (dataset_generation.py:80-90): input range
-    max - min + margin per level (dl_models.py:128-152), output range max - min per level."""
+    max - min + margin per level (dl_models.py:128-152); output range max - min of the level, at
+    every point of it (the reference's scaling_params carry a range per point; a few training
+    states do not determine one, so the library's training uses the level's)."""
     lo, hi = None, None
     for st in states:
-        cf = torch.stack([a.amin(dim=(1, 2)) for a in cell_fields(st)])
-        cx = torch.stack([a.amax(dim=(1, 2)) for a in cell_fields(st)])
-        lo = cf if lo is None else torch.minimum(lo, cf)
-        hi = cx if hi is None else torch.maximum(hi, cx)
+        mn, mx = level_extrema(st)
+        lo = mn if lo is None else torch.minimum(lo, mn)
+        hi = mx if hi is None else torch.maximum(hi, mx)
     nz, ny, nx = states[0][0].shape
-    m = torch.tensor(margins, device=lo.device).view(5, 1)
-    rout = (hi - lo).view(5, nz, 1, 1).expand(5, nz, ny, nx).contiguous()
+    m = torch.tensor(margins, device=lo.device, dtype=lo.dtype).view(5, 1)
+    rout = (hi - lo).view(5, nz + 1, 1, 1).expand(5, nz + 1, ny, nx).contiguous()
     return {"lo": lo.contiguous(), "rin": (hi - lo + m).contiguous(), "rout": rout}
 
 

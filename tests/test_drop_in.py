@@ -137,7 +137,7 @@ def test_sprint_dl_applies_the_correction_inside_the_step(built_lib):
         assert np.array_equal(a, b)
 
 
-def test_scaling_params_convert_to_level_ranges():
+def test_scaling_params_convert_to_the_library_layout():
     from lex_gb300 import one_sprint_functions as sp
     nx, ny, nz = 4, 3, 5
     r = np.random.default_rng(7)
@@ -149,30 +149,27 @@ def test_scaling_params_convert_to_level_ranges():
     ws, bs, out = sp.sgs_arrays(_flax_params(1), tuple(sc) + (None,) * 4, nx, ny, nz)
     assert [w.shape for w in ws] == [(27, 32, 16), (27, 32, 32), (27, 32, 32), (27, 8, 32)]
     assert not ws[0][:, :, 5:].any() and not ws[3][:, 5:, :].any() and not bs[3][5:].any()
+    assert out["lo"].shape == (5, nz + 1) and out["rout"].shape == (5, nz + 1, ny, nx)
+    top = lambda a: np.append(a, a[-1])                  # entry nz repeats the top level but for w
+    lvl = lambda a: np.concatenate([a, a[:, :, -1:]], axis=2)
     th_min, th_max = sc[0][0, 0], sc[1][0, 0]
-    assert np.allclose(out["lo"][0], th_min.min(axis=(0, 1)))
-    assert np.allclose(out["rin"][0], th_max.max(axis=(0, 1)) - th_min.min(axis=(0, 1)) + 0.01)
-    assert np.allclose(out["rout"][0], (th_max - th_min).transpose(2, 1, 0))
-    w_min, w_max = sc[6][0, 0], sc[7][0, 0]                # w on faces: the two faces of a cell averaged
-    lo_f = w_min.min(axis=(0, 1))
-    assert np.allclose(out["lo"][3], 0.5 * (lo_f[:-1] + lo_f[1:]))
-    rw = w_max - w_min
-    assert np.allclose(out["rout"][3], (0.5 * (rw[:, :, :-1] + rw[:, :, 1:])).transpose(2, 1, 0))
-    ru = sc[3][0, 0] - sc[2][0, 0]                          # u on x faces
-    assert np.allclose(out["rout"][1], (0.5 * (ru[:-1] + ru[1:])).transpose(2, 1, 0))
+    assert np.allclose(out["lo"][0], top(th_min.min(axis=(0, 1))))
+    assert np.allclose(out["rin"][0], top(th_max.max(axis=(0, 1)) - th_min.min(axis=(0, 1)) + 0.01))
+    assert np.allclose(out["rout"][0], lvl(th_max - th_min).transpose(2, 1, 0))
+    w_min, w_max = sc[6][0, 0], sc[7][0, 0]                # w per face level, faces 0..nz
+    assert np.allclose(out["lo"][3], w_min.min(axis=(0, 1)))
+    assert np.allclose(out["rout"][3], (w_max - w_min).transpose(2, 1, 0))
+    ru = sc[3][0, 0] - sc[2][0, 0]                          # u on x faces 0..nx-1
+    assert np.allclose(out["rout"][1], lvl(ru[:nx]).transpose(2, 1, 0))
     q_min, q_max = sc[8][0, 0], sc[9][0, 0]
-    assert np.allclose(out["rin"][4], q_max.max(axis=(0, 1)) - q_min.min(axis=(0, 1)) + 1e-5)
+    assert np.allclose(out["rin"][4], top(q_max.max(axis=(0, 1)) - q_min.min(axis=(0, 1)) + 1e-5))
 
 
 def test_dl_packing_matches_the_reference():
     """The network input and the applied correction against the reference's own
-    phys_state_tuple2array / correct_array2tuple (tests/golden/dl_packing.npz).  theta, u, v and qv
-    inputs agree to rounding (normalising faces then averaging, as the reference does, equals
-    averaging then normalising with the same level's range); w is normalised after averaging here,
-    so its input is not compared.  Corrections agree everywhere except on the periodic end faces,
-    where the reference copies a neighbouring face and this library takes the periodic mean (the
-    golden's output ranges depend on the level only, and for w not even on that: the library
-    scales cell-centred corrections before staggering them, the reference face corrections)."""
+    phys_state_tuple2array / correct_array2tuple (tests/golden/dl_packing.npz), all five channels and
+    every stored face (u and v faces 0..nx-1 / 0..ny-1: the reference's correction also changes the
+    duplicated periodic face nx / ny, to the value of face 1, which the device layout does not store)."""
     torch = pytest.importorskip("torch")
     from lex_gb300 import one_sprint_functions as sp, sgs_cnn
     g = load_golden("dl_packing.npz")
@@ -184,14 +181,14 @@ def test_dl_packing_matches_the_reference():
         g["in_" + f][3:3 + nx + e[0], 3:3 + ny + e[1], 1:1 + nz + e[2]].transpose(2, 1, 0))) for f, e in ext.items())
     x = sgs_cnn.pack(state, scale).numpy().reshape(nz, ny, nx, 5).transpose(2, 1, 0, 3)
     ref = g["packed"][0]
-    for c in (0, 1, 2, 4):
+    for c in range(5):
         assert np.allclose(x[..., c], ref[..., c], rtol=1e-12, atol=1e-12), c
     corr = torch.tensor(np.ascontiguousarray(g["corr"].transpose(2, 1, 0, 3).reshape(-1, 5)))
     d = [a.numpy() for a in sgs_cnn.unpack(corr, scale, (nx, ny, nz))]
     t = lambda a: a.transpose(2, 1, 0)
     assert np.allclose(d[0], t(g["out_theta"]), rtol=1e-12, atol=1e-12)
     assert np.allclose(d[5], t(g["out_qv"]), rtol=1e-12, atol=1e-12)
-    assert np.allclose(d[1][:, :, 1:], t(g["out_u"][1:nx]), rtol=1e-12, atol=1e-12)
-    assert np.allclose(d[2][:, 1:, :], t(g["out_v"][:, 1:ny]), rtol=1e-12, atol=1e-12)
+    assert np.allclose(d[1], t(g["out_u"][:nx]), rtol=1e-12, atol=1e-12)
+    assert np.allclose(d[2], t(g["out_v"][:, :ny]), rtol=1e-12, atol=1e-12)
     assert np.allclose(d[3], t(g["out_w"]), rtol=1e-12, atol=1e-12)
     assert not d[4].any()

@@ -29,53 +29,69 @@ def test_coarse_grain_means_over_cells_and_faces():
 
 
 def test_scale_is_per_level_with_margins():
-    from lex_gb300.sgs_cnn import cell_fields, make_scale
+    from lex_gb300.sgs_cnn import make_scale
     a, b = _state(4, 3, 5, 1), _state(4, 3, 5, 2)
     sc = make_scale([a, b])
-    assert sc["lo"].shape == (5, 5) and sc["rin"].shape == (5, 5) and sc["rout"].shape == (5, 5, 3, 4)
-    for f, (fa, fb) in enumerate(zip(cell_fields(a), cell_fields(b))):
-        for k in range(5):
-            lo = min(fa[k].min(), fb[k].min())
-            hi = max(fa[k].max(), fb[k].max())
+    nz = 5
+    assert sc["lo"].shape == (5, nz + 1) and sc["rin"].shape == (5, nz + 1) and sc["rout"].shape == (5, nz + 1, 3, 4)
+    for f, i in enumerate((0, 1, 2, 3, 5)):            # each field on its own points; w per face level
+        levels = nz + 1 if f == 3 else nz
+        for k in range(nz + 1):
+            kk = min(k, levels - 1)                     # entry nz repeats the top level but for w
+            lo = min(a[i][kk].min(), b[i][kk].min())
+            hi = max(a[i][kk].max(), b[i][kk].max())
             assert torch.isclose(sc["lo"][f, k], lo)
             margin = 1e-5 if f == 4 else 0.01
             assert torch.isclose(sc["rin"][f, k], hi - lo + margin)
             assert torch.allclose(sc["rout"][f, k], (hi - lo).expand(3, 4))
 
 
-def test_pack_normalises_cell_centred_fields():
-    from lex_gb300.sgs_cnn import cell_fields, make_scale, pack
+def test_pack_normalises_then_averages_the_winds():
+    """dl_models.phys_state_tuple2array: every field normalised on its own points (w per face
+    level), then u, v, w averaged to the cell centre."""
+    from lex_gb300.sgs_cnn import make_scale, pack
     st = _state(4, 3, 5, 3)
     sc = make_scale([st])
     x = pack(st, sc)
     assert x.shape == (60, 5)
-    for f, a in enumerate(cell_fields(st)):
-        ref = ((a - sc["lo"][f].view(-1, 1, 1)) / sc["rin"][f].view(-1, 1, 1)).reshape(-1)
-        assert torch.equal(x[:, f], ref)
-    # x fastest: point 1 is (k, j, i) = (0, 0, 1); ui there averages u faces 1 and 2
-    ui = 0.5 * (st[1][0, 0, 1] + st[1][0, 0, 2])
-    assert torch.isclose(x[1, 1], (ui - sc["lo"][1, 0]) / sc["rin"][1, 0])
+    lo, rin = sc["lo"], sc["rin"]
+    n = lambda a, f, m: (a - lo[f, :m].view(-1, 1, 1)) / rin[f, :m].view(-1, 1, 1)
+    assert torch.equal(x[:, 0], n(st[0], 0, 5).reshape(-1))
+    assert torch.equal(x[:, 4], n(st[5], 4, 5).reshape(-1))
+    wn = n(st[3], 3, 6)
+    assert torch.equal(x[:, 3], (0.5 * (wn[:-1] + wn[1:])).reshape(-1))
+    # x fastest: point 1 is (k, j, i) = (0, 0, 1); ui there averages the normalised u faces 1 and 2
+    un = lambda i: (st[1][0, 0, i] - lo[1, 0]) / rin[1, 0]
+    assert torch.isclose(x[1, 1], 0.5 * (un(1) + un(2)))
 
 
-def test_unpack_staggers_the_correction():
+def test_unpack_staggers_the_correction_as_the_reference():
+    """dl_models.correct_array2tuple / stagger_uvw: a face i >= 1 gets the mean of the cells beside
+    it, face 0 the value of face nx-1 (the face next to the far end), w zero on the bottom and the
+    lid; each field times its range at its own point."""
     from lex_gb300.sgs_cnn import unpack
     nx, ny, nz = 4, 3, 5
-    rout = torch.ones(5, nz, ny, nx, dtype=torch.float64) * torch.arange(1, 6, dtype=torch.float64).view(5, 1, 1, 1)
+    rout = torch.ones(5, nz + 1, ny, nx, dtype=torch.float64) * torch.arange(1, 6, dtype=torch.float64).view(5, 1, 1, 1)
     corr = torch.zeros(nx * ny * nz, 5, dtype=torch.float64)
     corr[:, 0] = 1.0
     cu = torch.zeros(nz, ny, nx, dtype=torch.float64)
-    cu[2, 1, 3] = 1.0                                  # one cell's u correction
+    cu[2, 1, 3] = 1.0                                  # the last cell of a row
     corr[:, 1] = cu.reshape(-1)
+    cv = torch.zeros(nz, ny, nx, dtype=torch.float64)
+    cv[1, 0, 2] = 1.0                                  # the first cell of a column
+    corr[:, 2] = cv.reshape(-1)
     cw = torch.zeros(nz, ny, nx, dtype=torch.float64)
     cw[0, 0, 0] = 1.0                                  # the bottom cell's w correction
     corr[:, 3] = cw.reshape(-1)
     th, u, v, w, p, q = unpack(corr, {"rout": rout}, (nx, ny, nz))
     assert torch.equal(th, torch.ones(nz, ny, nx, dtype=torch.float64))
-    # u faces west (i = 3) and east (i = 0, periodic) of the cell get half of it, times the range 2
+    # u: face 3 (west of cell 3) gets half, times the range 2; face 0 copies face 3 (face nx-1)
     assert u[2, 1, 3] == 1.0 and u[2, 1, 0] == 1.0 and float(u.abs().sum()) == 2.0
+    # v: face 1 (north of cell 0) gets half, times 3; face 0 copies face ny-1 = 2, which is zero
+    assert v[1, 1, 2] == 1.5 and float(v.abs().sum()) == 1.5
     # w: interior face 1 gets half of the bottom cell's correction (range 4); face 0 stays zero
     assert w[1, 0, 0] == 2.0 and float(w.abs().sum()) == 2.0 and float(w[0].abs().sum()) == 0.0
-    assert float(v.abs().sum()) == 0.0 and float(p.abs().sum()) == 0.0 and float(q.abs().sum()) == 0.0
+    assert float(p.abs().sum()) == 0.0 and float(q.abs().sum()) == 0.0
 
 
 def test_bubble_generators():
