@@ -203,10 +203,11 @@ int lexgb_budget_noalloc(int nx, int ny, int nz, double dx, double dy, double dz
                          const float *const fields[6], const double *rho0_col, const double *pi0_col,
                          double *out, void *stream);
 
-/* Message of the last failure on this thread; returns the untruncated length. */
-/* The prognostic state in the device layout: interior only, x fastest; theta (K), u, v, pi', qv
+/* The prognostic state in the device layout: interior only, x fastest; theta, u, v, pi', qv
  * [nz][ny][nx] and w [nz+1][ny][nx], FP32, host (on_device = 0) or device pointers (1, e.g. torch
- * CUDA tensors; ordered on the context's stream).  set marks the state as present.
+ * CUDA tensors; ordered on the context's stream), theta in K; on_device = 2: device pointers with theta
+ * as the device stores it, theta - theta_ref (no rounding of theta to FP32 kelvin: the exact state).
+ * set marks the state as present.
  * The device-pointer form of lexgb_upload_state / lexgb_download_state (no reference counterpart:
  * LEX hands JAX arrays around, one_sprint_functions.py:10-30). */
 int lexgb_set_state_interior(lexgb_ctx *ctx, const float *const fields[6], int on_device);
@@ -286,6 +287,7 @@ int lexgb_cnn_adam(long long n, float *w, const float *gw, float *m, float *v, v
 int lexgb_set_sgs_net(lexgb_ctx *ctx, const void *const w[4], const float *const b[4], const float *in_lo,
                       const float *in_range, const float *out_range, int enable);
 
+/* Message of the last failure on this thread; returns the untruncated length. */
 int lexgb_last_error(char *buf, size_t len);
 
 #ifdef __cplusplus

@@ -13,9 +13,11 @@ Smagorinsky constant can be an input too (``step(solver, state, cs=tensor)``): i
 the library's FP64 accumulation of the derivative through every step's eddy viscosity.
 
 State layout: a tuple of six float32 CUDA tensors in the device layout, x fastest -
-theta [K], u, v, pi', qv of shape (nz, ny, nx) and w of shape (nz+1, ny, nx) (u on west faces,
-v on south faces, w on faces 0..nz).  There is no CPU path: without a GPU and the built
-library the calls raise.
+theta, u, v, pi', qv of shape (nz, ny, nx) and w of shape (nz+1, ny, nx) (u on west faces,
+v on south faces, w on faces 0..nz).  theta is in K, or with ``raw=True`` relative to the
+solver's theta_ref as the device stores it (exact: FP32 kelvin rounds theta to about 3e-5 K, so a
+rollout in kelvin re-rounds the state at every step boundary).  There is no CPU path: without a GPU
+and the built library the calls raise.
 """
 import ctypes
 
@@ -50,31 +52,33 @@ def _bind_stream(solver):
     solver.set_stream(h if h else 1)
 
 
-def set_state(solver, tensors):
-    """Copy a device-layout state into the solver (ordered on torch's current stream)."""
+def set_state(solver, tensors, raw=False):
+    """Copy a device-layout state into the solver (ordered on torch's current stream); raw: theta
+    relative to theta_ref."""
     tensors = tuple(t.contiguous() for t in tensors)
     _check(solver, tensors)
     _bind_stream(solver)
-    _lib.check(solver.lib.lexgb_set_state_interior(solver.handle, _ptrs(tensors), 1))
+    _lib.check(solver.lib.lexgb_set_state_interior(solver.handle, _ptrs(tensors), 2 if raw else 1))
 
 
-def get_state(solver):
-    """The solver's state as new device-layout tensors."""
+def get_state(solver, raw=False):
+    """The solver's state as new device-layout tensors; raw: theta relative to theta_ref."""
     out = tuple(torch.empty(s, dtype=torch.float32, device="cuda") for s in _shapes(solver))
     _bind_stream(solver)
-    _lib.check(solver.lib.lexgb_get_state_interior(solver.handle, _ptrs(out), 1))
+    _lib.check(solver.lib.lexgb_get_state_interior(solver.handle, _ptrs(out), 2 if raw else 1))
     return out
 
 
 class _Step(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, solver, cs, *state):
+    def forward(ctx, solver, cs, raw, *state):
         if cs is not None and float(cs) != solver.cs:
             _bind_stream(solver)
             solver.set_cs(float(cs))
         ctx.with_cs = cs is not None
         ctx.cs = solver.cs      # the backward differentiates the step with this step's Cs
-        set_state(solver, state)
+        ctx.raw = raw
+        set_state(solver, state, raw)
         _bind_stream(solver)
         _lib.check(solver.lib.lexgb_step_keep(solver.handle))
         solver._keep_count = getattr(solver, "_keep_count", 0) + 1
@@ -82,7 +86,7 @@ class _Step(torch.autograd.Function):
         ctx.token = solver._kept_token
         ctx.solver = solver
         ctx.save_for_backward(*state)
-        return get_state(solver)
+        return get_state(solver, raw)
 
     @staticmethod
     def backward(ctx, *grads):
@@ -99,25 +103,26 @@ class _Step(torch.autograd.Function):
         if getattr(solver, "_kept_token", None) == ctx.token:   # this step's intermediates are still kept
             _lib.check(solver.lib.lexgb_step_vjp_kept(solver.handle, _ptrs(gy), _ptrs(gx), 1))
         else:                                                   # recompute from the saved input
-            set_state(solver, ctx.saved_tensors)
+            set_state(solver, ctx.saved_tensors, ctx.raw)
             _lib.check(solver.lib.lexgb_step_vjp(solver.handle, 3, _ptrs(gy), _ptrs(gx), 1))
         solver._kept_token = None
         if solver.cs != cs_now:
             solver.set_cs(cs_now)
         gcs = torch.tensor(solver.cs_grad(reset=True), dtype=torch.float64, device="cuda") if ctx.with_cs else None
-        return (None, gcs) + gx
+        return (None, gcs, None) + gx
 
 
-def step(solver, state, cs=None):
+def step(solver, state, cs=None, raw=False):
     """One differentiable big step: state -> next state (tuples of six CUDA tensors); cs: an
-    optional scalar tensor, the Smagorinsky constant of the step, differentiable."""
+    optional scalar tensor, the Smagorinsky constant of the step, differentiable; raw: theta
+    relative to the solver's theta_ref (see the module docstring)."""
     if not isinstance(solver, Solver):
         raise TypeError("solver must be a lex_gb300.solver.Solver")
-    return _Step.apply(solver, cs, *state)
+    return _Step.apply(solver, cs, bool(raw), *state)
 
 
-def rollout(solver, state, nsteps, cs=None):
+def rollout(solver, state, nsteps, cs=None, raw=False):
     """nsteps differentiable big steps (the sprint of one_sprint_functions.py:109-115)."""
     for _ in range(int(nsteps)):
-        state = step(solver, state, cs)
+        state = step(solver, state, cs, raw)
     return state

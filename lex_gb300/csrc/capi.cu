@@ -1057,7 +1057,7 @@ int lexgb_set_state_interior(lexgb_ctx* c, const float* const fields[6], int on_
     CK(cudaMemcpyAsync(field_of(c->A, f), fields[f], n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                        c->stream));
   }
-  CK(launch_shift(c->A.T, -(float)c->theta_ref, (size_t)c->d.cells(), c->stream));
+  if (on_device != 2) CK(launch_shift(c->A.T, -(float)c->theta_ref, (size_t)c->d.cells(), c->stream));
   c->state_set = true;
   if (!on_device) CK(cudaStreamSynchronize(c->stream));
   return LEXGB_OK;
@@ -1069,7 +1069,7 @@ int lexgb_get_state_interior(lexgb_ctx* c, float* fields[6], int on_device) {
   for (int f = 0; f < NFIELD; ++f) {
     if (!fields[f]) return fail(LEXGB_ERR_ARG, "null field pointer");
     const size_t n = (f == 3 ? c->d.faces() : c->d.cells()) * sizeof(float);
-    if (f == 0 && on_device) {
+    if (f == 0 && on_device == 1) {
       CK(cudaMemcpyAsync(fields[0], c->A.T, n, cudaMemcpyDeviceToDevice, c->stream));
       CK(launch_shift(fields[0], (float)c->theta_ref, (size_t)c->d.cells(), c->stream));
       continue;

@@ -8,7 +8,8 @@ constant, checked against central finite differences (the differentiable-step ca
 The backward runs the library's reverse mode through lex_gb300.autograd with a checkpoint every
 `seg` steps (torch.utils.checkpoint over segments: only every seg-th state is kept, a segment
 is recomputed in the backward pass).  Finite differences use the library's graph forward
-(FP32) on seeded random directions v of the initial theta (unit normal per point) and on Cs:
+(FP32, theta kept relative to theta_ref) on seeded random directions v of the initial theta (unit
+normal per point) and on Cs (tests/test_gpu_gradcheck.py takes them from the FP64 oracle instead):
     <dL/dtheta0, v>  vs  (L(theta0 + eps v) - L(theta0 - eps v)) / (2 eps)
     dL/dCs           vs  (L(Cs + eps) - L(Cs - eps)) / (2 eps)
 
@@ -32,28 +33,31 @@ def experiment(n=64, spacing=(300.0, 300.0, 150.0), dt=2.0, steps=300, seg=10, n
     S = Solver(n, n, n, *spacing, dt, 32, turb_opt=1)
     phys, prof = warm_bubble(n, n, n, *spacing, amplitude=2.0, seed=seed)
     S.integrate_base_state(prof["theta0"], prof["qv0"])
+    # theta in the device layout (theta - theta_ref, exact in FP32) throughout: the loss's theta'
+    # = theta - 300 K is that plus a constant
+    off = float(prof["theta0"][1]) - 300.0
     S.upload(phys, dtype=np.float32)
-    x0 = lag.get_state(S)
+    x0 = lag.get_state(S, raw=True)
     phys_t, _ = warm_bubble(n, n, n, *spacing, amplitude=2.5, seed=seed)
     S.upload(phys_t, dtype=np.float32)
     S.step(steps)
-    target = lag.get_state(S)[0] - 300.0
+    target = lag.get_state(S, raw=True)[0].double() + off
 
     def loss_nograd(theta0, cs):
         if cs != S.cs:
             S.set_cs(cs)
-        lag.set_state(S, (theta0,) + tuple(x0[1:]))
+        lag.set_state(S, (theta0,) + tuple(x0[1:]), raw=True)
         S.step(steps)
-        th = lag.get_state(S)[0]
-        return float(((th - 300.0 - target).double() ** 2).mean())
+        th = lag.get_state(S, raw=True)[0]
+        return float(((th.double() + off - target) ** 2).mean())
 
     # gradient by the reverse mode, checkpoint every seg steps
     theta0 = x0[0].clone().requires_grad_(True)
     cs = torch.tensor(cs0, dtype=torch.float64, device="cuda", requires_grad=True)
     state = (theta0,) + tuple(x0[1:])
     for _ in range(steps // seg):
-        state = checkpoint(lambda *s: lag.rollout(S, s, seg, cs), *state, use_reentrant=False)
-    L = ((state[0] - 300.0 - target) ** 2).mean()
+        state = checkpoint(lambda *s: lag.rollout(S, s, seg, cs, raw=True), *state, use_reentrant=False)
+    L = ((state[0].double() + off - target) ** 2).mean()
     L.backward()
     g_theta, g_cs = theta0.grad.detach().double(), float(cs.grad)
     t_grad = time.time() - t0

@@ -18,27 +18,43 @@ with the tuples of ``setup_lex.setup_grid_n_ic`` (setup_lex.py:66-69):
 The grid sizes, spacings, dt, n_sound and sprint_n come from the namelist module, as in the
 reference (``namelist_n_constants``, imported on first use, or the object given to
 :func:`configure`).  Like the reference, the functions return new padded arrays and never
-modify their inputs.  The solver and its device state persist across calls: a state returned
-by :func:`ws_rk3_sprint` and passed back unchanged is not uploaded again.
+modify their inputs.  The solver and its device state persist across calls: the state a sprint
+returns stays on the device (:class:`ResidentField` objects, read like NumPy arrays), a state passed
+back unchanged is not uploaded again, and the host copy is made when something reads the arrays -
+for ``lex_relay.py`` that is ``write.save2nc`` (write_netcdf.py:56-57), one download of the six
+fields per save.
 
 Only solver_opt 2 with damping, radiation and surface fluxes off and turb_opt 0 or 1 is
 implemented on the GPU; other options raise ``NotImplementedError`` (no CPU fallback).
 """
-import numpy as np
+import weakref
 
-from .solver import Solver
+import numpy as np
+from numpy.lib.mixins import NDArrayOperatorsMixin
+
+from .solver import Solver, FIELDS, padded_shape
 
 _nl = None
 _solver = None
 _key = None
-_last = None   # (returned tuple, id of its arrays) of the last sprint
+_last = None   # weak reference to the state the last call returned (still on the device)
 _sgs = None    # (ids of dl_params and scaling_params, device tensors) of the attached network
+
+
+def _retire_last():
+    """Keep the last returned state readable before the device state it refers to changes."""
+    global _last
+    prev = _last() if _last is not None else None
+    if prev is not None:
+        prev.preserve()
+    _last = None
 
 
 def configure(namelist):
     """Use ``namelist`` (any object with nx, ny, nz, dx, dy, dz, dt, n_sound, sprint_n and,
     when cor_opt is on, fCor) instead of importing ``namelist_n_constants``."""
     global _nl, _solver, _key, _last, _sgs
+    _retire_last()
     _nl = namelist
     if _solver is not None:
         _solver.close()
@@ -76,6 +92,7 @@ def _ensure(base_state, model_opt):
     key = (int(nl.nx), int(nl.ny), int(nl.nz), float(nl.dx), float(nl.dy), float(nl.dz), float(nl.dt),
            int(nl.n_sound), cor_opt, turb_opt, float(getattr(nl, "fCor", 1.0e-4)))
     if _solver is None or key != _key:
+        _retire_last()
         if _solver is not None:
             _solver.close()
         _solver = Solver(key[0], key[1], key[2], key[3], key[4], key[5], key[6], key[7], turb_opt=turb_opt,
@@ -86,9 +103,9 @@ def _ensure(base_state, model_opt):
     # invalidates the resident phys_state
     cols = tuple(np.asarray(base_state[i], dtype=np.float64)[0, 0, :].copy() for i in (2, 4, 3, 1))
     if _solver._base_cols is None or not all(np.array_equal(a, b) for a, b in zip(cols, _solver._base_cols)):
+        _retire_last()
         _solver.set_base_state(base_state)
         _solver._base_cols = cols
-        _last = None
     return _solver
 
 
@@ -99,18 +116,138 @@ def _sfc_zeros():
     return (-999, -999, z(), z(), z(), z(), z(), z(), z())
 
 
+class _ResidentState:
+    """The six fields a sprint left on the device.  The host copy (padded reference layout, one
+    download of all six fields) is made on first read and is read-only, as JAX arrays are
+    immutable.  Before the solver advances past this state, an unread state is copied on the
+    device (``preserve``), so it can still be read afterwards."""
+    downloads = 0   # host copies made (all states), for tests and for tracing IO
+
+    def __init__(self, solver, dtype):
+        self.solver = solver
+        self.dtype = dtype
+        self.host = None
+        self.snap = None
+
+    def preserve(self):
+        if self.host is None and self.snap is None:
+            self.snap = [_device_copy(p, n) for p, n in zip(self.solver.device_ptrs(), _counts(self.solver))]
+            self.theta_ref = _theta_ref(self.solver)
+
+    def materialize(self):
+        if self.host is None:
+            if self.snap is None:
+                host = self.solver.download(self.dtype)
+            else:
+                host = _pad_host(self.snap, self.theta_ref, self.solver, self.dtype)
+                self.snap = None
+            for a in host:
+                a.setflags(write=False)
+            self.host = host
+            _ResidentState.downloads += 1
+        return self.host
+
+
+class ResidentField(NDArrayOperatorsMixin):
+    """One field of a sprint's result on the device, in the reference's padded [x][y][z] layout.
+
+    Reads like a NumPy array (``np.asarray``, slicing, ``np.reshape``, arithmetic); the first read of
+    any field of the state copies all six to the host.  Read-only: to change a state, make a new
+    array (JAX arrays are immutable too)."""
+
+    def __init__(self, state, index):
+        self._state = state
+        self._index = index
+        nx, ny, nz = state.solver.nx, state.solver.ny, state.solver.nz
+        self.shape = padded_shape(nx, ny, nz, FIELDS[index])
+        self.dtype = np.dtype(state.dtype)
+        self.ndim = 3
+        self.size = int(np.prod(self.shape))
+
+    def __array__(self, dtype=None, copy=None):
+        a = self._state.materialize()[self._index]
+        if dtype is not None and np.dtype(dtype) != a.dtype:
+            return a.astype(dtype)
+        return a.copy() if copy else a
+
+    def __getitem__(self, idx):
+        return np.asarray(self)[idx]
+
+    def __len__(self):
+        return self.shape[0]
+
+    def __array_ufunc__(self, ufunc, method, *inputs, **kwargs):
+        inputs = tuple(np.asarray(x) if isinstance(x, ResidentField) else x for x in inputs)
+        return getattr(ufunc, method)(*inputs, **kwargs)
+
+    def __repr__(self):
+        where = "host" if self._state.host is not None else "device"
+        return "ResidentField(%s, shape=%s, dtype=%s, on %s)" % (FIELDS[self._index], self.shape, self.dtype, where)
+
+
+class _DeviceArray:
+    """A device allocation seen by torch without a copy (``__cuda_array_interface__``)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f4", "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def _device_copy(ptr, n):
+    """A device-to-device copy of the n FP32 values at ``ptr``, ordered after the solver's work."""
+    import torch
+    if _solver is not None:
+        _solver.synchronize()
+    out = torch.as_tensor(_DeviceArray(ptr, n), device="cuda").clone()
+    torch.cuda.current_stream().synchronize()   # before the solver writes its state again
+    return out
+
+
+def _counts(solver):
+    nx, ny, nz = solver.nx, solver.ny, solver.nz
+    return [nx * ny * (nz + 1) if f == 3 else nx * ny * nz for f in range(6)]
+
+
+def _theta_ref(solver):
+    """The constant the device subtracts from theta (lexgb_config.theta_ref, else theta0 at level 1)."""
+    return float(solver.cfg.theta_ref) if solver.cfg.theta_ref != 0.0 else float(solver._base[0][1])
+
+
+def _pad_host(snap, theta_ref, solver, dtype):
+    """Device-layout copies -> the padded reference layout on the host, as lexgb_download_state makes it."""
+    from .workload import _pad
+    nx, ny, nz = solver.nx, solver.ny, solver.nz
+    out = []
+    for f, t in enumerate(snap):
+        a = t.cpu().numpy().astype(np.float64).reshape((nz + 1 if f == 3 else nz), ny, nx).transpose(2, 1, 0)
+        if f == 0:
+            a = a + theta_ref
+        if f == 1:
+            a = np.concatenate([a, a[:1]], 0)
+        if f == 2:
+            a = np.concatenate([a, a[:, :1]], 1)
+        out.append(np.ascontiguousarray(_pad(a, "u" if f == 1 else ("v" if f == 2 else "s")), dtype=dtype))
+    return tuple(out)
+
+
 def _advance(phys_state, base_state, model_opt, nsteps, sgs=None):
     global _last
     s = _ensure(base_state, model_opt)
     _attach(s, sgs)
-    resident = _last is not None and len(phys_state) == 6 and all(a is b for a, b in zip(phys_state, _last))
-    if not resident:
+    prev = _last() if _last is not None else None
+    resident = prev is not None and len(phys_state) == 6 and all(
+        isinstance(a, ResidentField) and a._state is prev for a in phys_state)
+    if resident:
+        prev.preserve()              # the caller may still read it after this sprint
+    else:
+        if prev is not None:
+            prev.preserve()
         s.upload(tuple(np.asarray(a) for a in phys_state))
+    dtype = np.result_type(*(np.dtype(a.dtype) for a in phys_state))
     s.step(nsteps)
-    dtype = np.result_type(*(np.asarray(a).dtype for a in phys_state))
-    out = s.download(np.float64 if dtype == np.float64 else np.float32)
-    _last = out
-    return out
+    st = _ResidentState(s, np.float64 if dtype == np.float64 else np.float32)
+    _last = weakref.ref(st)
+    return tuple(ResidentField(st, f) for f in range(6))
 
 
 def sgs_arrays(dl_params, scaling_params, nx, ny, nz):

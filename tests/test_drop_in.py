@@ -192,3 +192,58 @@ def test_dl_packing_matches_the_reference():
     assert np.allclose(d[2], t(g["out_v"][:, :ny]), rtol=1e-12, atol=1e-12)
     assert np.allclose(d[3], t(g["out_w"]), rtol=1e-12, atol=1e-12)
     assert not d[4].any()
+
+
+@pytest.mark.gpu
+def test_relay_sequence_keeps_the_state_on_the_device(built_lib, tmp_path):
+    """lex_relay.py's calls (lex_relay.py:17-61) through the drop-in on the 32^3 warm bubble at
+    600 m / dt 3 s for 600 s (the CPU-runnable case): get_first_step_flux, save2nc_base, save2nc, then
+    sprints of 20 steps with a save every 5 sprints.  The state stays on the device between sprints:
+    one host copy of the six fields per save and none in between.  The final state matches the
+    reference's own 600 s run (tests/golden/bubble32_600s.npz) as test_gpu_parity's 600 s case does;
+    a state read after later sprints (kept by the caller) still holds its own values; host copies
+    are read-only."""
+    from lex_gb300 import one_sprint_functions as sp, write_netcdf as write
+    from oracle.ic import WarmBubble
+    g = load_golden("bubble32_600s.npz")
+    nx, ny, nz = int(g["nx"]), int(g["ny"]), int(g["nz"])
+    bubble = lambda: WarmBubble(nx, ny, nz, float(g["dx"]), float(g["dy"]), float(g["dz"]), seed=int(g["seed"])).build()
+    phys, base, grids = bubble()
+    nl = types.SimpleNamespace(nx=nx, ny=ny, nz=nz, dx=float(g["dx"]), dy=float(g["dy"]), dz=float(g["dz"]),
+                               dt=float(g["dt"]), n_sound=int(g["n_sound"]), sprint_n=20, fCor=1.0e-4,
+                               file_name_format=str(tmp_path / "lex_%04d.nc"), base_file_name=str(tmp_path / "base.nc"),
+                               output_format=1, sfc_opt=0, pic_opt=0)
+    sp.configure(nl)
+    sfc = sp.get_first_step_flux(phys, base, grids, OK)
+    write.save2nc_base(base, grids)
+    write.save2nc(phys, sfc, grids, 0, 0.0)
+    d0 = sp._ResidentState.downloads
+    relay_n, save_n = int(g["nsteps"]) // nl.sprint_n, 5
+    kept = None
+    for i in range(relay_n):
+        phys, sfc = sp.ws_rk3_sprint(phys, base, grids, OK)
+        if i == 2:
+            kept = phys                                   # read only after later sprints
+        if (i + 1) % save_n == 0:
+            write.save2nc(phys, sfc, grids, (i + 1) // save_n, (i + 1) * nl.sprint_n * nl.dt)
+    assert sp._ResidentState.downloads - d0 == relay_n // save_n    # one host copy per save
+    th = np.asarray(phys[0])
+    assert not th.flags.writeable
+    with pytest.raises(ValueError):
+        th[0, 0, 0] = 0.0
+    saved = np.load(str(tmp_path / ("lex_%04d.npz" % (relay_n // save_n))))
+    np.testing.assert_array_equal(saved["theta"][0], th[3:-3, 3:-3, 1:-1].astype(np.float32))
+    inner = (slice(3, -3), slice(3, -3), slice(1, -1))
+    qv0 = base[4][inner]
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    errs = {"theta_p": rel(th[inner] - 300.0, g["theta_p"]), "qv_p": rel(np.asarray(phys[5])[inner] - qv0, g["qv_p"]),
+            "w": rel(np.asarray(phys[3])[3:-3, 3:-3, 1:-1], g["w"])}
+    assert errs["theta_p"] < 1e-3 and errs["qv_p"] < 1e-3 and errs["w"] < 2e-3, errs
+    # the state of sprint 3, read now: 60 steps from the start, unaffected by the later sprints
+    sp.configure(nl)
+    again = bubble()[0]
+    for _ in range(3):
+        again, _ = sp.ws_rk3_sprint(again, base, grids, OK)
+    for a, b in zip(kept, again):
+        np.testing.assert_array_equal(np.asarray(a), np.asarray(b))
+    sp.configure(nl)
