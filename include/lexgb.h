@@ -196,7 +196,8 @@ int lexgb_time_kernel(lexgb_ctx *ctx, int which, int reps, float *ms_per_launch)
  * legacy default stream), not synchronised.  Partial sums go to a fixed array of
  * LEXGB_NOALLOC_MAX_BLOCKS x 4 doubles (256 KiB) compiled into the library, one slot per 2048
  * cells: grids above 16,777,216 cells are rejected with LEXGB_ERR_ARG.  The first call on a
- * device looks up that array's device address (make it before any stream capture); all calls
+ * device looks up that array's device address (make it before any stream capture) and keeps it for
+ * the life of the process, so it is not valid after a cudaDeviceReset of that device; all calls
  * share the array, so calls that overlap on the GPU race. */
 #define LEXGB_NOALLOC_MAX_BLOCKS 8192
 int lexgb_budget_noalloc(int nx, int ny, int nz, double dx, double dy, double dz, double theta_ref,

@@ -19,7 +19,9 @@
 //
 // Set-up: the device address of the array is looked up with cudaGetSymbolAddress once per
 // device, by the first call made while that device is current; make that first call before any
-// stream capture.
+// stream capture.  The address is kept for the life of the process: after a cudaDeviceReset of a
+// device (which unloads this library's device code there) the kept address no longer names the
+// array, so a process that resets a device must not call lexgb_budget_noalloc on it again.
 #include <cuda_runtime.h>
 
 #include <mutex>
