@@ -175,8 +175,9 @@ int lexgb_step_kernel_count(lexgb_ctx *ctx, int *n_kernels);
  * events (state untouched: outputs go to scratch).  *ms_per_launch = average launch duration. */
 enum {
     LEXGB_KERNEL_ACOUSTIC = 0,  /* one acoustic sub-step */
-    LEXGB_KERNEL_DIV_TRHO,      /* mass divergence + theta_rho */
-    LEXGB_KERNEL_ADV_SCALARS,   /* theta and qv advection + Euler update */
+    LEXGB_KERNEL_DIV_TRHO,      /* mass divergence + theta_rho (a kernel of its own only where nx % 4 != 0) */
+    LEXGB_KERNEL_ADV_SCALARS,   /* theta and qv advection + Euler update; forms the mass divergence and
+                                   theta_rho on the way, as a stage runs it */
     LEXGB_KERNEL_ADV_MOMENTUM,  /* u, v, w advection + Coriolis + buoyancy + SGS -> R_u, R_v, R_w */
     LEXGB_KERNEL_SMAG_A,
     LEXGB_KERNEL_SMAG_B,

@@ -192,11 +192,12 @@ int run_smag(lexgb_ctx* c, const State& x, float* n2, float* km) {
 int run_stage(lexgb_ctx* c, int s, const State& xi0, const State& xis, const State& out, float* dT, float* dq) {
   const StagePlan p = plan_of(c->cfg);
   const bool sgs_on = c->cfg.turb_opt == 1;
-  CK(launch_div_trho(c->d, c->ph, c->cols, xis, c->div, c->trho, c->stream));
   Sgs sg{nullptr, nullptr, nullptr, nullptr, nullptr};
   if (sgs_on) sg = Sgs{c->sgs[0], c->sgs[1], c->sgs[2], c->sgs[3], c->sgs[4]};
   SlowOut so{nullptr, nullptr, nullptr, out.T, out.q, dT, dq};
-  CK(launch_adv_scalars(c->d, c->ph, c->cols, xis, c->div, xi0.T, xi0.q, sg, (float)p.dts[s], so, c->stream));
+  // theta/qv advection, which also forms div(rho0 u) and theta_rho of the stage state
+  CK(launch_adv_scalars(c->d, c->ph, c->cols, xis, nullptr, xi0.T, xi0.q, sg, (float)p.dts[s], so, c->stream,
+                        c->div, c->trho));
   CK(launch_adv_momentum(c->d, c->ph, c->cols, xis, c->div, sg, c->Ru, c->Rv, c->Rw, 0, c->stream));
   // acoustic sub-steps from xi0's winds and pi'; pi'_s is the stage state's pi'.  With
   // acoustic_pairs, sub-steps go two per launch (an odd count starts with a single one).
@@ -364,7 +365,8 @@ int build_table(lexgb_ctx* c) {
   CK(launch_build_columns(nz, c->cfg.dz, c->theta_ref, c->base64, c->base64 + S, c->base64 + 2 * S,
                           c->base64 + 3 * S, c->tab, c->stream));
   float* t = c->tab;
-  c->cols = Cols{t, t + S, t + 2 * S, t + 3 * S, t + 4 * S, t + 5 * S, t + 6 * S, t + 7 * S, t + 8 * S, t + 9 * S};
+  c->cols = Cols{t,         t + S,     t + 2 * S, t + 3 * S, t + 4 * S,  t + 5 * S,
+                 t + 6 * S, t + 7 * S, t + 8 * S, t + 9 * S, t + 10 * S, t + 11 * S};
   c->base_set = true;
   c->adj_kept = false;
   drop_graph(c);
@@ -492,7 +494,7 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
   for (int i = 0; i < 3; ++i) c->diag[i] = take();
   e = cudaMalloc(&c->base64, 4 * (cfg->nz + 2) * sizeof(double));
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("base columns: ") + cudaGetErrorString(e));
-  e = cudaMalloc(&c->tab, 10 * (cfg->nz + 2) * sizeof(float));
+  e = cudaMalloc(&c->tab, kColumnRows * (cfg->nz + 2) * sizeof(float));
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("column table: ") + cudaGetErrorString(e));
   e = cudaMalloc(&c->partial, (size_t)budget_blocks(c->d) * 4 * sizeof(double));
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("budget partials: ") + cudaGetErrorString(e));
@@ -1011,8 +1013,9 @@ int lexgb_time_kernel(lexgb_ctx* c, int which, int reps, float* ms_per_launch) {
         return launch_acoustic_persist(d, c->ph, c->cols, io, c->stream, c->l2on ? &c->l2win : nullptr);
       }
       case LEXGB_KERNEL_DIV_TRHO: return launch_div_trho(d, c->ph, c->cols, x, c->div, c->trho, c->stream);
-      case LEXGB_KERNEL_ADV_SCALARS:
-        return launch_adv_scalars(d, c->ph, c->cols, x, c->div, x.T, x.q, sg, (float)p.dts[2], so, c->stream);
+      case LEXGB_KERNEL_ADV_SCALARS:   // as a stage runs it: also forming div(rho0 u) and theta_rho
+        return launch_adv_scalars(d, c->ph, c->cols, x, nullptr, x.T, x.q, sg, (float)p.dts[2], so, c->stream,
+                                  c->div, c->trho);
       case LEXGB_KERNEL_ADV_MOMENTUM:
         return launch_adv_momentum(d, c->ph, c->cols, x, c->div, sg, c->Ru, c->Rv, c->Rw, 0, c->stream);
       case LEXGB_KERNEL_SMAG_A: return launch_smag_a(d, c->ph, c->cols, x, t, c->stream);
@@ -1209,9 +1212,9 @@ int adj_forward(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages) {
   for (int s = 0; s < nstages; ++s) {
     const State xs = s == 0 ? A : w.S[s];
     const State& out = w.S[s + 1];
-    CK(launch_div_trho(d, c->ph, c->cols, xs, w.div[s], w.trho[s], c->stream));
     SlowOut so{nullptr, nullptr, nullptr, out.T, out.q, nullptr, nullptr};
-    CK(launch_adv_scalars(d, c->ph, c->cols, xs, w.div[s], A.T, A.q, sg, (float)p.dts[s], so, c->stream));
+    CK(launch_adv_scalars(d, c->ph, c->cols, xs, nullptr, A.T, A.q, sg, (float)p.dts[s], so, c->stream, w.div[s],
+                          w.trho[s]));
     CK(launch_adv_momentum(d, c->ph, c->cols, xs, w.div[s], sg, w.Ru[s], w.Rv[s], w.Rw[s], 0, c->stream));
     AcousticIn in{A.u, A.v, A.w, A.p, w.Ru[s], w.Rv[s], w.Rw[s], w.trho[s], xs.p};
     for (int m = 1; m <= p.n[s]; ++m) {

@@ -43,15 +43,15 @@ __device__ __forceinline__ float weno5_grad(float a, float b, float c, float d, 
   const float b2 = (13.f / 12.f) * t3 * t3 + 0.25f * t4 * t4;
   const float b3 = (13.f / 12.f) * t5 * t5 + 0.25f * t6 * t6;
   const float dd = b1 - b3, tau = fabsf(dd), sg = dd >= 0.f ? 1.f : -1.f;
-  // one approximate reciprocal per denominator (the forward divides with __fdividef too)
-  const float i1 = __fdividef(1.f, b1 + eps), i2 = __fdividef(1.f, b2 + eps), i3 = __fdividef(1.f, b3 + eps);
+  // one approximate reciprocal per denominator (the forward divides with div_approx)
+  const float i1 = rcp_approx(b1 + eps), i2 = rcp_approx(b2 + eps), i3 = rcp_approx(b3 + eps);
   const float q1r = tau * i1, q2r = tau * i2, q3r = tau * i3;
   const float r1 = fminf(kRatioCap, q1r), r2 = fminf(kRatioCap, q2r), r3 = fminf(kRatioCap, q3r);
   const float w1 = 0.1f * (1.f + r1 * r1), w2 = 0.6f * (1.f + r2 * r2), w3 = 0.3f * (1.f + r3 * r3);
   const float q1 = (2.f / 6.f) * a + (-7.f / 6.f) * b + (11.f / 6.f) * c;
   const float q2 = (-1.f / 6.f) * b + (5.f / 6.f) * c + (2.f / 6.f) * d;
   const float q3 = (2.f / 6.f) * c + (5.f / 6.f) * d + (-1.f / 6.f) * e;
-  const float iS = __fdividef(1.f, w1 + w2 + w3);
+  const float iS = rcp_approx(w1 + w2 + w3);
   const float W = (w1 * q1 + w2 * q2 + w3 * q3) * iS;
   // reverse
   const float qb1 = w1 * iS, qb2 = w2 * iS, qb3 = w3 * iS;
@@ -79,12 +79,12 @@ __device__ __forceinline__ float weno3_grad(float a, float b, float c, float eps
   const float dab = a - b, dbc = b - c;
   const float b1 = dab * dab, b2 = dbc * dbc;
   const float dd = b1 - b2, tau = fabsf(dd), sg = dd >= 0.f ? 1.f : -1.f;
-  const float i1 = __fdividef(1.f, b1 + eps), i2 = __fdividef(1.f, b2 + eps);
+  const float i1 = rcp_approx(b1 + eps), i2 = rcp_approx(b2 + eps);
   const float q1r = tau * i1, q2r = tau * i2;
   const float r1 = fminf(kRatioCap, q1r), r2 = fminf(kRatioCap, q2r);
   const float w1 = (1.f / 3.f) * (1.f + r1 * r1), w2 = (2.f / 3.f) * (1.f + r2 * r2);
   const float q1 = -0.5f * a + 1.5f * b, q2 = 0.5f * b + 0.5f * c;
-  const float iS = __fdividef(1.f, w1 + w2);
+  const float iS = rcp_approx(w1 + w2);
   const float W = (w1 * q1 + w2 * q2) * iS;
   const float qb1 = w1 * iS, qb2 = w2 * iS;
   const float wb1 = (q1 - W) * iS, wb2 = (q2 - W) * iS;

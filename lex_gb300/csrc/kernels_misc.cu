@@ -101,10 +101,13 @@ __global__ void k_build_columns(int nz, double dz, double theta_ref, const doubl
   float* d0 = tab + 7 * S;
   float* pic = tab + 8 * S;
   float* dpi0dz = tab + 9 * S;
+  float* rho_inv = tab + 10 * S;
+  float* rho_w_inv = tab + 11 * S;
   for (int f = threadIdx.x; f <= nz; f += blockDim.x) {
     if (f < nz) {
       const int L = f + 1;
       rho[f] = (float)rho0[L];
+      rho_inv[f] = (float)(1.0 / (double)(float)rho0[L]);
       theta0[f] = (float)th0[L];
       qv0[f] = (float)q0[L];
       trho0[f] = (float)(th0[L] * (1.0 + kReps * q0[L]) / (1.0 + q0[L]));
@@ -123,6 +126,8 @@ __global__ void k_build_columns(int nz, double dz, double theta_ref, const doubl
       we = rf;
     rho_wext[f] = (float)we;
     dpi0dz[f] = (float)((pi0[f + 1] - pi0[f]) / dz);
+    // the face density of w's advective tendency, formed in FP32 as the kernels form it
+    rho_w_inv[f] = (f == 0 || f == nz) ? 0.f : (float)(1.0 / (double)(0.5f * ((float)rho0[f] + (float)rho0[f + 1])));
   }
 }
 

@@ -64,6 +64,8 @@ struct Cols {
   const float* d0;        // nz    theta0 - theta_ref
   const float* pi0;       // nz
   const float* dpi0dz;    // nz+1  (pi0_pad[f+1] - pi0_pad[f]) / dz
+  const float* rho_inv;   // nz    1 / rho (of the FP32 rho), correctly rounded
+  const float* rho_w_inv; // nz+1  1 / (0.5f * (rho[f-1] + rho[f])) on interior faces, 0 at f = 0 and nz
 };
 
 struct Phys {
@@ -82,6 +84,20 @@ __device__ __forceinline__ int clampi(int i, int lo, int hi) { return i < lo ? l
 // reconstruction (advection.py:305-416 and the lateral blocks :424-503)
 // ---------------------------------------------------------------------------------------------
 // WENO5 value at the face right of c; a..e ordered upwind -> downwind.
+// Approximate reciprocal and quotient (PTX rcp.approx / div.approx, flush-to-zero forms: every
+// operand here is a normal number, b + eps >= 1e-18 and weight sums >= 0.1, where the non-ftz forms
+// give the same result but spend extra instructions on the subnormal range).
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float div_approx(float x, float y) {
+  float r;
+  asm("div.approx.ftz.f32 %0, %1, %2;" : "=f"(r) : "f"(x), "f"(y));
+  return r;
+}
+
 __device__ __forceinline__ float weno5(float a, float b, float c, float d, float e, float eps) {
   const float t1 = a - 2.f * b + c, t2 = a - 4.f * b + 3.f * c;
   const float t3 = b - 2.f * c + d, t4 = b - d;
@@ -90,16 +106,16 @@ __device__ __forceinline__ float weno5(float a, float b, float c, float d, float
   const float b2 = (13.f / 12.f) * t3 * t3 + 0.25f * t4 * t4;
   const float b3 = (13.f / 12.f) * t5 * t5 + 0.25f * t6 * t6;
   const float tau = fabsf(b1 - b3);
-  const float r1 = fminf(kRatioCap, __fdividef(tau, b1 + eps));
-  const float r2 = fminf(kRatioCap, __fdividef(tau, b2 + eps));
-  const float r3 = fminf(kRatioCap, __fdividef(tau, b3 + eps));
+  const float r1 = fminf(kRatioCap, div_approx(tau, b1 + eps));
+  const float r2 = fminf(kRatioCap, div_approx(tau, b2 + eps));
+  const float r3 = fminf(kRatioCap, div_approx(tau, b3 + eps));
   const float w1 = 0.1f * (1.f + r1 * r1);
   const float w2 = 0.6f * (1.f + r2 * r2);
   const float w3 = 0.3f * (1.f + r3 * r3);
   const float q1 = (2.f / 6.f) * a + (-7.f / 6.f) * b + (11.f / 6.f) * c;
   const float q2 = (-1.f / 6.f) * b + (5.f / 6.f) * c + (2.f / 6.f) * d;
   const float q3 = (2.f / 6.f) * c + (5.f / 6.f) * d + (-1.f / 6.f) * e;
-  return __fdividef(w1 * q1 + w2 * q2 + w3 * q3, w1 + w2 + w3);
+  return div_approx(w1 * q1 + w2 * q2 + w3 * q3, w1 + w2 + w3);
 }
 
 // WENO3 value at the face right of b; a, b, c = s[-1], s[0], s[+1] upwind-ordered.
@@ -107,11 +123,11 @@ __device__ __forceinline__ float weno3(float a, float b, float c, float eps) {
   const float b1 = (a - b) * (a - b);
   const float b2 = (b - c) * (b - c);
   const float tau = fabsf(b1 - b2);
-  const float r1 = fminf(kRatioCap, __fdividef(tau, b1 + eps));
-  const float r2 = fminf(kRatioCap, __fdividef(tau, b2 + eps));
+  const float r1 = fminf(kRatioCap, div_approx(tau, b1 + eps));
+  const float r2 = fminf(kRatioCap, div_approx(tau, b2 + eps));
   const float w1 = (1.f / 3.f) * (1.f + r1 * r1);
   const float w2 = (2.f / 3.f) * (1.f + r2 * r2);
-  return __fdividef(w1 * (-0.5f * a + 1.5f * b) + w2 * (0.5f * b + 0.5f * c), w1 + w2);
+  return div_approx(w1 * (-0.5f * a + 1.5f * b) + w2 * (0.5f * b + 0.5f * c), w1 + w2);
 }
 
 // Vertical face value between column entries f-1 and f of an n-entry column s(0..n-1),
@@ -155,11 +171,7 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float rcp_approx(float x) {
-  float r;
-  asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
+
 __device__ __forceinline__ float2 rcp2(float2 x) { return make_float2(rcp_approx(x.x), rcp_approx(x.y)); }
 __device__ __forceinline__ float2 sel2(bool p, float2 a, float2 b) { return p ? a : b; }
 
@@ -269,8 +281,11 @@ struct Sgs {
 };
 
 cudaError_t launch_div_trho(const Dims&, const Phys&, const Cols&, State in, float* div, float* trho, cudaStream_t);
+// div_out / trho_out: when given, the divergence div(rho0 u) and theta_rho of `in` are computed here
+// (inside the vertical-march kernel where it runs, else by launch_div_trho first) and `div` is unused
 cudaError_t launch_adv_scalars(const Dims&, const Phys&, const Cols&, State in, const float* div, const float* T0,
-                               const float* q0, Sgs sgs, float dts, SlowOut out, cudaStream_t);
+                               const float* q0, Sgs sgs, float dts, SlowOut out, cudaStream_t,
+                               float* div_out = nullptr, float* trho_out = nullptr);
 // once per process, before the first launch (opts the momentum kernel into > 48 KB of shared memory)
 cudaError_t init_weno_attributes();
 // u, v, w together; wmode 0: R_w = adv_w + b8w + sgs_w; 1: adv_w only; 2: b8w only
@@ -357,6 +372,7 @@ cudaError_t launch_export_interior(const Dims&, const float* src, int kind, doub
 // FP64 base state
 cudaError_t launch_hydrostatic(int nz, double dz, const double* theta0, const double* qv0, double* pi0,
                                double* rho0, cudaStream_t);
+constexpr int kColumnRows = 12;   // rows of nz + 2 floats in the column table (the Cols fields, in order)
 cudaError_t launch_build_columns(int nz, double dz, double theta_ref, const double* theta0, const double* qv0,
                                  const double* pi0, const double* rho0, float* table, cudaStream_t);
 // FP64 budgets: partial sums per block into `partial` (nblocks x 4), then a final pass into out[4]

@@ -3,7 +3,9 @@
 The golden vectors use 16x12x8, 16x16x12 and 32^3 grids.  These cases add nx not a multiple of
 4 (the kernels' scalar staging paths), nx not a multiple of the 32-wide tiles, ny smaller than
 a tile's halo reach, and nz = 1 and 2 (mod 4), where the last vertical tile holds one or two
-levels and the one-sided top extrapolations reach below the tile.  The oracle (FP64) is the
+levels and the one-sided top extrapolations reach below the tile.  8 x 5 x 7 and the smallest
+grid the library accepts, 4 x 4 x 6, put a 32 x 8 tile and its halo across several periods of
+the grid (wrapped by full modulo).  The oracle (FP64) is the
 reference; it is pinned to the reference's own outputs by tests/test_oracle_golden.py.
 """
 import pytest
@@ -13,7 +15,7 @@ from test_gpu_parity import FIELDS, inner, state_err
 
 pytestmark = pytest.mark.gpu
 
-GRIDS = [(18, 10, 13), (20, 7, 14), (36, 6, 9)]
+GRIDS = [(18, 10, 13), (20, 7, 14), (36, 6, 9), (8, 5, 7), (4, 4, 6)]
 
 
 def _case(nx, ny, nz, seed=5):
