@@ -121,16 +121,18 @@ def build_case(nx, ny, nz, dx, dy, dz, **_):
 SAMPLE = (48, 48, GRID["nz"])
 
 
-def _oracle_worker(k, warm, barrier, out):
-    """One core: `warm` RK3 steps of the oracle on the sample sub-domain, a barrier with the other
-    cores, then `k` timed steps; puts the CLOCK_MONOTONIC start and end of the timed steps."""
+def _oracle_worker(k, warm, barrier, out, dtype="f32"):
+    """One core: `warm` RK3 steps of the oracle (NumPy, FP32 or FP64 arithmetic) on the sample
+    sub-domain, a barrier with the other cores, then `k` timed steps; puts the CLOCK_MONOTONIC
+    start and end of the timed steps."""
     from oracle.ic import WarmBubble, Grid
     from oracle.dycore import Dycore
     nx, ny, nz = SAMPLE
     phys, base, _ = WarmBubble(nx, ny, nz, GRID["dx"], GRID["dy"], GRID["dz"]).build()
     cols = dict(theta0=base[2][0, 0], qv0=base[4][0, 0], pi0=base[3][0, 0], rho0=base[1][0, 0])
-    D = Dycore(Grid(nx, ny, nz, GRID["dx"], GRID["dy"], GRID["dz"]), cols, GRID["dt"], GRID["n_sound"])
-    st = phys
+    D = Dycore(Grid(nx, ny, nz, GRID["dx"], GRID["dy"], GRID["dz"]), cols, GRID["dt"], GRID["n_sound"],
+               dtype=np.float32 if dtype == "f32" else np.float64)
+    st = D.cast(phys)
     for _ in range(warm):
         st, _ = D.step(st)
     barrier.wait(timeout=600)
@@ -140,14 +142,14 @@ def _oracle_worker(k, warm, barrier, out):
     out.put((t0, time.monotonic()))
 
 
-def oracle_throughput(k, warm):
+def oracle_throughput(k, warm, dtype="f32"):
     """The oracle on every host core at once (spawned processes, one sample sub-domain each, timed
     together after a barrier): (grid-pt-steps/s over the union of the timed windows, cores, s)."""
     import multiprocessing as mp
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
     ctx = mp.get_context("spawn")
     barrier, out = ctx.Barrier(cores), ctx.Queue()
-    procs = [ctx.Process(target=_oracle_worker, args=(k, warm, barrier, out)) for _ in range(cores)]
+    procs = [ctx.Process(target=_oracle_worker, args=(k, warm, barrier, out, dtype)) for _ in range(cores)]
     for p in procs:
         p.start()
     try:
@@ -160,17 +162,22 @@ def oracle_throughput(k, warm):
     return pts / (t1 - t0), cores, t1 - t0
 
 
-def _sample_text(k, cores, seconds):
+def _sample_text(k, cores, seconds, dtype="f32"):
     nx, ny, nz = SAMPLE
     return ("%d RK3 step(s) of a %dx%dx%d sub-domain of the workload (same dz, dt, physics) on each of %d host "
-            "cores at once (one process per core), NumPy FP64 restatement of the reference (oracle/; the reference "
-            "is Python/JAX and not installable here), %.1f s" % (k, nx, ny, nz, cores, seconds))
+            "cores at once (one process per core), NumPy %s restatement of the reference (oracle/; the reference "
+            "is Python/JAX and not installable here), %.1f s" % (k, nx, ny, nz, cores,
+                                                                 "FP32" if dtype == "f32" else "FP64", seconds))
 
 
 def cpu_baseline():
-    """The oracle (NumPy, FP64) on every host core, a bounded sample of the workload."""
-    value, cores, sec = oracle_throughput(2, 1)
-    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": _sample_text(2, cores, sec)}
+    """The oracle (NumPy) on every host core, a bounded sample of the workload: in FP32, the
+    reference's precision, and (second line) in FP64."""
+    value, cores, sec = oracle_throughput(2, 1, "f32")
+    v64, c64, s64 = oracle_throughput(2, 1, "f64")
+    return {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "dtype": "f32",
+            "sample": _sample_text(2, cores, sec, "f32"),
+            "fp64": {"value": v64, "unit": UNIT, "cores": c64, "sample": _sample_text(2, c64, s64, "f64")}}
 
 
 def run_reference(args):
@@ -179,12 +186,12 @@ def run_reference(args):
         return
     k = min(max(1, args.steps), 3)
     warm = max(0, min(args.warmup, 1))
-    value, cores, sec = oracle_throughput(k, warm)
-    sample = _sample_text(k, cores, sec)
+    value, cores, sec = oracle_throughput(k, warm, "f32")
+    sample = _sample_text(k, cores, sec, "f32")
     nx, ny, _ = SAMPLE
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": k,
             "warmup": warm, "ms_per_step": 1e3 * GRID["nx"] * GRID["ny"] * GRID["nz"] / value,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "impl": "reference",
             "config": {"workload": "warm bubble 192x192x96 @ 100 m, dt = 1 s (sampled on %dx%dx%d per core)"
                                    % SAMPLE, "grid": [GRID["nx"], GRID["ny"], GRID["nz"]]},
@@ -433,6 +440,33 @@ def profile_sgs(args):
     print(json.dumps({"profile_sgs": True, "steps": args.steps, "warmup": args.warmup}))
 
 
+def profile_adjoint(args):
+    """Warm-up + timed forward-with-intermediates + reverse passes of the benchmarked step
+    (lexgb_step_keep + lexgb_step_vjp_kept), for profiler captures."""
+    import ctypes
+    import torch
+    from lex_gb300.solver import Solver
+    from lex_gb300 import _lib
+    g = GRID
+    phys, profile = build_case(**g)
+    S = Solver(g["nx"], g["ny"], g["nz"], g["dx"], g["dy"], g["dz"], g["dt"], g["n_sound"], turb_opt=1)
+    S.integrate_base_state(profile["theta0"], profile["qv0"])
+    S.upload(phys, dtype=np.float32)
+    shp = [(g["nz"], g["ny"], g["nx"])] * 6
+    shp[3] = (g["nz"] + 1, g["ny"], g["nx"])
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    ybar = [torch.randn(sh, device="cuda", generator=gen) for sh in shp]
+    xbar = [torch.empty(sh, device="cuda") for sh in shp]
+    yp = (ctypes.c_void_p * 6)(*[t.data_ptr() for t in ybar])
+    xp = (ctypes.c_void_p * 6)(*[t.data_ptr() for t in xbar])
+    for _ in range(args.warmup + args.steps):
+        _lib.check(S.lib.lexgb_step_keep(S.handle))
+        _lib.check(S.lib.lexgb_step_vjp_kept(S.handle, yp, xp, 1))
+    torch.cuda.synchronize()
+    S.close()
+    print(json.dumps({"profile_adjoint": True, "steps": args.steps, "warmup": args.warmup}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -445,11 +479,15 @@ def main():
     ap.add_argument("--profile", action="store_true", help="only warm-up + timed steps (profiler captures)")
     ap.add_argument("--profile-sgs", action="store_true",
                     help="only a few coarse 32^3 steps with the fused learned SGS correction (profiler captures)")
+    ap.add_argument("--profile-adjoint", action="store_true",
+                    help="only forward-with-intermediates + reverse passes of the step (profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "lexgb":
         args.warmup = 3
     if args.profile_sgs:
         profile_sgs(args)
+    elif args.profile_adjoint:
+        profile_adjoint(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -140,7 +140,9 @@ int lexgb_diagnose(lexgb_ctx *ctx, int what, double *host_out);
  * out[0] total air mass  sum rho dV (rho from pi0+pi', theta, qv as get_rho, :941-947)
  * out[1] water vapour mass  sum rho qv dV
  * out[2] kinetic energy  sum 0.5 rho0 (u^2+v^2+w^2) dV (velocities averaged to cell centres)
- * out[3] sum rho0 theta dV.  n_out >= 4. */
+ * out[3] sum rho0 theta dV
+ * out[4] total energy  sum rho (cv T + g z + 0.5 (u^2+v^2+w^2)) dV, T = (pi0+pi') theta, z the cell
+ *        centre's height, cv of dry air; written when n_out >= 5.  n_out >= 4. */
 int lexgb_budget(lexgb_ctx *ctx, double *out, int n_out);
 
 /* Non-finite check of the state: *n_bad = number of non-finite values (0 = clean). */

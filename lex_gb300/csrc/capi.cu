@@ -496,9 +496,9 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("base columns: ") + cudaGetErrorString(e));
   e = cudaMalloc(&c->tab, kColumnRows * (cfg->nz + 2) * sizeof(float));
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("column table: ") + cudaGetErrorString(e));
-  e = cudaMalloc(&c->partial, (size_t)budget_blocks(c->d) * 4 * sizeof(double));
+  e = cudaMalloc(&c->partial, (size_t)budget_blocks(c->d) * kBudgetSums * sizeof(double));
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("budget partials: ") + cudaGetErrorString(e));
-  e = cudaMalloc(&c->budget, 4 * sizeof(double));
+  e = cudaMalloc(&c->budget, kBudgetSums * sizeof(double));
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("budget: ") + cudaGetErrorString(e));
   e = cudaMalloc(&c->count, sizeof(unsigned long long));
   if (e != cudaSuccess) return bail(LEXGB_ERR_ALLOC, std::string("counter: ") + cudaGetErrorString(e));
@@ -905,7 +905,8 @@ int lexgb_budget(lexgb_ctx* c, double* out, int n_out) {
   const size_t S = c->d.nz + 2;
   CK(launch_budget(c->d, c->ph, c->cols, c->A, c->base64 + 3 * S, c->base64 + 2 * S, c->theta_ref, c->partial,
                    c->budget, c->stream));
-  CK(cudaMemcpyAsync(out, c->budget, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(out, c->budget, (n_out < kBudgetSums ? n_out : kBudgetSums) * sizeof(double),
+                     cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return LEXGB_OK;
 }

@@ -140,11 +140,12 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// sums of the budget (kBudgetSums doubles per block, then one final sum each)
 __global__ void __launch_bounds__(RED_THREADS) k_budget_partial(Dims d, Phys ph, Cols c, State s,
                                                               const double* __restrict__ rho0_col,
                                                               const double* __restrict__ pi0_col, double theta_ref,
                                                               double* __restrict__ partial) {
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  double acc[kBudgetSums] = {0.0, 0.0, 0.0, 0.0, 0.0};
   const long long n = d.cells();
   const double dV = (double)ph.dx * (double)ph.dy * (double)ph.dz;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
@@ -160,45 +161,48 @@ __global__ void __launch_bounds__(RED_THREADS) k_budget_partial(Dims d, Phys ph,
     const double uc = 0.5 * ((double)s.u[t] + (double)s.u[d.at(wrap(i + 1, d.nx), j, k)]);
     const double vc = 0.5 * ((double)s.v[t] + (double)s.v[d.at(i, wrap(j + 1, d.ny), k)]);
     const double wc = 0.5 * ((double)s.w[t] + (double)s.w[d.at(i, j, k + 1)]);
+    const double ke = 0.5 * (uc * uc + vc * vc + wc * wc);
     acc[0] += rho * dV;
     acc[1] += rho * qv * dV;
-    acc[2] += 0.5 * r0 * (uc * uc + vc * vc + wc * wc) * dV;
+    acc[2] += r0 * ke * dV;
     acc[3] += r0 * th * dV;
+    // total energy: internal (cv T, T = pi theta) + potential (g z at the cell centre) + kinetic
+    acc[4] += rho * (kCv * (pi * th) + kG * ((k + 0.5) * (double)ph.dz) + ke) * dV;
   }
-  __shared__ double sm[4][RED_THREADS / 32];
+  __shared__ double sm[kBudgetSums][RED_THREADS / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int m = 0; m < 4; ++m) {
+  for (int m = 0; m < kBudgetSums; ++m) {
     const double v = warp_sum(acc[m]);
     if (lane == 0) sm[m][wid] = v;
   }
   __syncthreads();
   if (wid == 0) {
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < kBudgetSums; ++m) {
       double v = lane < RED_THREADS / 32 ? sm[m][lane] : 0.0;
       v = warp_sum(v);
-      if (lane == 0) partial[blockIdx.x * 4 + m] = v;
+      if (lane == 0) partial[blockIdx.x * kBudgetSums + m] = v;
     }
   }
 }
 
 __global__ void k_budget_final(int nblocks, const double* __restrict__ partial, double* __restrict__ out) {
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  double acc[kBudgetSums] = {0.0, 0.0, 0.0, 0.0, 0.0};
   for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
 #pragma unroll
-    for (int m = 0; m < 4; ++m) acc[m] += partial[b * 4 + m];
-  __shared__ double sm[4][RED_THREADS / 32];
+    for (int m = 0; m < kBudgetSums; ++m) acc[m] += partial[b * kBudgetSums + m];
+  __shared__ double sm[kBudgetSums][RED_THREADS / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int m = 0; m < 4; ++m) {
+  for (int m = 0; m < kBudgetSums; ++m) {
     const double v = warp_sum(acc[m]);
     if (lane == 0) sm[m][wid] = v;
   }
   __syncthreads();
   if (wid == 0) {
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < kBudgetSums; ++m) {
       double v = lane < RED_THREADS / 32 ? sm[m][lane] : 0.0;
       v = warp_sum(v);
       if (lane == 0) out[m] = v;

@@ -377,6 +377,7 @@ cudaError_t launch_build_columns(int nz, double dz, double theta_ref, const doub
                                  const double* pi0, const double* rho0, float* table, cudaStream_t);
 // FP64 budgets: partial sums per block into `partial` (nblocks x 4), then a final pass into out[4]
 int budget_blocks(const Dims&);
+constexpr int kBudgetSums = 5;   // mass, vapour, kinetic energy, rho0 theta, total energy
 cudaError_t launch_budget(const Dims&, const Phys&, const Cols&, State in, const double* rho0_col,
                           const double* pi0_col, double theta_ref, double* partial, double* out, cudaStream_t);
 cudaError_t launch_count_nonfinite(const float* a, long long n, unsigned long long* count, cudaStream_t);

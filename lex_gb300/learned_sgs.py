@@ -352,6 +352,11 @@ def experiment_large(net_state=None, iters=300, chunk=50, lr=3e-5, sprints=2, t_
             "cost_ratio": cost_learned / cost_plain, "seconds": time.time() - t0, "net": net, "scale": scale}
 
 
+def _host(scale):
+    """A scale dict with its tensors on the host (the Laplacian ranges are plain floats)."""
+    return {k: (v.cpu() if torch.is_tensor(v) else v) for k, v in scale.items()}
+
+
 def main(argv=None):
     import argparse
     import json
@@ -377,14 +382,14 @@ def main(argv=None):
                        laplacian_terms=a.laplacian, neg_qv=a.neg_qv)
         net, scale = r.pop("net"), r.pop("scale")
         state = net.state_dict()
-        nets["32"] = {"net": state, "scale": {k: v.cpu() for k, v in scale.items()}}
+        nets["32"] = {"net": state, "scale": _host(scale)}
         lines.append(json.dumps(r))
         print(lines[-1], flush=True)
     if a.case in ("128", "both"):
         r = experiment_large(net_state=state, iters=a.iters_large, lr=a.lr, sprints=a.sprints,
                              laplacian_terms=a.laplacian, neg_qv=a.neg_qv)
         net, scale = r.pop("net"), r.pop("scale")
-        nets["128"] = {"net": net.state_dict(), "scale": {k: v.cpu() for k, v in scale.items()}}
+        nets["128"] = {"net": net.state_dict(), "scale": _host(scale)}
         lines.append(json.dumps(r))
         print(lines[-1], flush=True)
     if a.out:

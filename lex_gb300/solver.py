@@ -232,9 +232,11 @@ class Solver:
         return out
 
     def budget(self):
-        out = np.empty(4)
-        check(self.lib.lexgb_budget(self.handle, _dptr(out), 4))
-        return dict(mass=out[0], vapour=out[1], kinetic=out[2], rho_theta=out[3])
+        """FP64 global sums of the current state: air mass, water vapour mass, kinetic energy
+        (0.5 rho0 |u|^2), rho0 theta and total energy (rho (cv T + g z + 0.5 |u|^2))."""
+        out = np.empty(5)
+        check(self.lib.lexgb_budget(self.handle, _dptr(out), 5))
+        return dict(mass=out[0], vapour=out[1], kinetic=out[2], rho_theta=out[3], total_energy=out[4])
 
     def count_nonfinite(self):
         n = ctypes.c_longlong()

@@ -1,7 +1,13 @@
 """The learned SGS correction inside the library's step (lexgb_set_sgs_net) against the
-differentiable PyTorch path used for training (lex_gb300.autograd step + sgs_cnn.correct), and
-training through the solver: a few Adam steps on one coarse-grained sprint lower its loss."""
+differentiable PyTorch path used for training (lex_gb300.autograd step + sgs_cnn.correct);
+training through the solver: a few Adam steps on one coarse-grained sprint lower its loss; and
+what a trained network (tests/golden/sgs_net_32.npz) gains over Smagorinsky alone on a held-out run."""
+import json
+
+import numpy as np
 import pytest
+
+from conftest import report_path
 
 pytestmark = pytest.mark.gpu
 
@@ -97,3 +103,46 @@ def test_training_through_the_solver_lowers_the_sprint_loss(built_lib):
             after = float(L.loss_fn(out, snaps[1], scale))
     assert all(h == h for h in hist)                 # finite
     assert after < hist[0], (hist[0], after)
+
+
+def _stored_network():
+    """The network and packing ranges of tests/golden/sgs_net_32.npz (tests/golden/make_sgs_net.py)."""
+    import torch
+    from conftest import load_golden
+    from lex_gb300 import sgs_cnn
+    g = load_golden("sgs_net_32.npz")
+    nw = sum(1 for k in g if k[0] == "w" and k[1:].isdigit())
+    net = sgs_cnn.SGSNet(seed=0)
+    net.load_state_dict({"w": [torch.from_numpy(g["w%d" % i]) for i in range(nw)],
+                         "b": [torch.from_numpy(g["b%d" % i]) for i in range(nw)]})
+    lo = torch.from_numpy(g["lo"]).cuda()
+    rin = torch.from_numpy(g["rin"]).cuda()
+    rl = torch.from_numpy(g["rout_level"]).cuda()
+    return net, lo, rin, rl, json.loads(str(g["summary"]))
+
+
+def test_trained_network_beats_smagorinsky_on_the_held_out_run(built_lib):
+    """What the learned correction gains (one_sprint_functions.py:118-165 applied after every
+    coarse step): on the held-out 600 s run (a bubble the training never saw; 100 m truth
+    coarse-grained to 600 m x 600 m x 300 m), the relative L2 error of theta' of the corrected
+    coarse run is below that of the run with Smagorinsky alone, by at least 20% on average, and
+    a corrected step costs at most 1.3 plain ones."""
+    from lex_gb300 import learned_sgs as L
+    from lex_gb300.workload import random_bubbles
+    net, lo, rin, rl, summary = _stored_network()
+    held = L.fine_run(random_bubbles(300, 1, 19200.0, 19200.0, centred=True), 300)
+    S = L.coarse_solver()
+    with S:
+        nz, ny, nx = held[0][0].shape
+        scale = {"lo": lo, "rin": rin, "rout": rl.view(5, nz + 1, 1, 1).expand(5, nz + 1, ny, nx).contiguous()}
+        base = L.theta_error(S, held)
+        learned = L.theta_error(S, held, net, scale)
+        plain_ms = L.step_cost(S, held[0])
+        corr_ms = L.step_cost(S, held[0], net, scale)
+    with open(report_path("learned_sgs_report.json"), "w") as f:
+        json.dump({"theta_err_smagorinsky": base, "theta_err_learned": learned,
+                   "mean_smagorinsky": float(np.mean(base)), "mean_learned": float(np.mean(learned)),
+                   "ms_per_step_plain": plain_ms, "ms_per_step_learned": corr_ms,
+                   "training_summary": {k: summary[k] for k in ("chosen", "cost_ratio", "seconds")}}, f, indent=1)
+    assert np.mean(learned) <= 0.8 * np.mean(base), (np.mean(learned), np.mean(base))
+    assert corr_ms <= 1.3 * plain_ms, (corr_ms, plain_ms)
