@@ -230,7 +230,8 @@ def run_lexgb(args):
 
     g = GRID
     phys, profile = build_case(**g)
-    S = Solver(g["nx"], g["ny"], g["nz"], g["dx"], g["dy"], g["dz"], g["dt"], g["n_sound"], turb_opt=1)
+    S = Solver(g["nx"], g["ny"], g["nz"], g["dx"], g["dy"], g["dz"], g["dt"], g["n_sound"], turb_opt=1,
+               acoustic_kernel=args.acoustic_kernel)
     stream = torch.cuda.Stream()
     S.set_stream(stream.cuda_stream)
     S.integrate_base_state(profile["theta0"], profile["qv0"])   # FP64 hydrostatic balance on the GPU
@@ -391,6 +392,7 @@ def run_lexgb(args):
                                "1+16+32 acoustic sub-steps, WENO5, Smagorinsky Cs=0.18",
                    "grid": [g["nx"], g["ny"], g["nz"]], "dx_m": g["dx"], "dt_s": g["dt"], "n_sound": g["n_sound"],
                    "l2": "inputs larger than L2: ~0.7 GB of fields touched per step vs 129 MB L2",
+                   "acoustic_form": S.acoustic_form,
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "kernel": "k_acoustic (one acoustic sub-step)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -479,6 +481,8 @@ def main():
     ap.add_argument("--profile", action="store_true", help="only warm-up + timed steps (profiler captures)")
     ap.add_argument("--profile-sgs", action="store_true",
                     help="only a few coarse 32^3 steps with the fused learned SGS correction (profiler captures)")
+    ap.add_argument("--acoustic-kernel", default="auto", choices=["auto", "rows", "tile", "persistent"],
+                    help="form of the acoustic sub-steps (auto: the fastest measured for the grid)")
     ap.add_argument("--profile-adjoint", action="store_true",
                     help="only forward-with-intermediates + reverse passes of the step (profiler captures)")
     args = ap.parse_args()
