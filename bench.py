@@ -365,21 +365,30 @@ def run_lexgb(args):
     if not args.no_sgs:
         from lex_gb300 import learned_sgs as lsgs, sgs_cnn, autograd as lag
         from lex_gb300.workload import warm_bubble
-        Sc = lsgs.coarse_solver(dims=(32, 32, 32))
-        cphys, _ = warm_bubble(32, 32, 32, 600.0, 600.0, 300.0)
-        Sc.upload(cphys, dtype=np.float32)
-        Sc.step(20)
-        xc = lag.get_state(Sc)
         net = sgs_cnn.SGSNet(seed=0, zero_last=False)
         net.w[3] *= 0.01   # corrections of the size a trained network makes
         net.refresh()
-        cplain = lsgs.step_cost(Sc, xc, n=300)
-        clearn = lsgs.step_cost(Sc, xc, net, sgs_cnn.make_scale([xc]), n=300)
-        Sc.close()
+
+        def corrected_cost(dims, n):
+            Sc = lsgs.coarse_solver(dims=dims)
+            cphys, _ = warm_bubble(*dims, 600.0, 600.0, 300.0)
+            Sc.upload(cphys, dtype=np.float32)
+            Sc.step(20)
+            xc = lag.get_state(Sc)
+            cplain = lsgs.step_cost(Sc, xc, n=n)
+            clearn = lsgs.step_cost(Sc, xc, net, sgs_cnn.make_scale([xc]), n=n)
+            Sc.close()
+            return cplain, clearn
+
+        cplain, clearn = corrected_cost((32, 32, 32), 300)
+        lplain, llearn = corrected_cost((128, 128, 64), 100)
         sgs = {"grid": [32, 32, 32], "dx_m": [600.0, 600.0, 300.0], "dt_s": 3.0,
                "ms_per_step_plain": cplain, "ms_per_step_learned": clearn, "cost_ratio": clearn / cplain,
-               "note": "CNN 5-32-32-32-5 (3x3x3, BF16 tensor cores) applied after every big step inside the "
-                       "step's CUDA graph (lexgb_set_sgs_net); CUDA events over 300 steps each"}
+               "grid_128x128x64": {"ms_per_step_plain": lplain, "ms_per_step_learned": llearn,
+                                   "cost_ratio": llearn / lplain},
+               "note": "CNN 5-32-32-32-5 (3x3x3, BF16 tensor cores: tcgen05 where the grid fits its tiles) "
+                       "applied after every big step inside the step's CUDA graph (lexgb_set_sgs_net); CUDA "
+                       "events over 300 (32^3) and 100 (128x128x64) steps each"}
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -421,12 +430,14 @@ def run_lexgb(args):
 
 
 def profile_sgs(args):
-    """Warm-up + timed coarse steps (32^3, 600 m x 600 m x 300 m) with the fused CNN correction."""
+    """Warm-up + timed coarse steps (600 m x 600 m x 300 m; 32^3 or --sgs-dims) with the fused CNN
+    correction."""
     import torch
     from lex_gb300 import learned_sgs as lsgs, sgs_cnn, autograd as lag
     from lex_gb300.workload import warm_bubble
-    S = lsgs.coarse_solver(dims=(32, 32, 32))
-    phys, _ = warm_bubble(32, 32, 32, 600.0, 600.0, 300.0)
+    dims = tuple(int(v) for v in args.sgs_dims.split(","))
+    S = lsgs.coarse_solver(dims=dims)
+    phys, _ = warm_bubble(*dims, 600.0, 600.0, 300.0)
     S.upload(phys, dtype=np.float32)
     S.step(args.warmup)
     x = lag.get_state(S)
@@ -481,6 +492,7 @@ def main():
     ap.add_argument("--profile", action="store_true", help="only warm-up + timed steps (profiler captures)")
     ap.add_argument("--profile-sgs", action="store_true",
                     help="only a few coarse 32^3 steps with the fused learned SGS correction (profiler captures)")
+    ap.add_argument("--sgs-dims", default="32,32,32", help="nx,ny,nz of --profile-sgs")
     ap.add_argument("--acoustic-kernel", default="auto", choices=["auto", "rows", "tile", "persistent"],
                     help="form of the acoustic sub-steps (auto: the fastest measured for the grid)")
     ap.add_argument("--profile-adjoint", action="store_true",

@@ -263,6 +263,17 @@ int lexgb_step_vjp_kept(lexgb_ctx *ctx, const float *const ybar[6], float *xbar[
  * Replace flax's Conv / optax in lex_dl_train.py (the reference trains with optax.lamb). */
 int lexgb_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const void *x, const void *w, const float *bias,
                      float *pre, void *y_bf16, float *y_f32, int gelu, int creal, void *stream);
+/* Which kernel the convolutions (lexgb_cnn_conv3d and the correction inside lexgb_step) use,
+ * process-wide: LEXGB_CNN_AUTO (default) the tcgen05 kernel (5th-generation tensor cores,
+ * accumulators in tensor memory, tiles of 8 x 16 points: nx % 8 == 0, ny % 16 == 0) where the grid
+ * fits it and has at least 2^18 points, else the mma.sync kernel; LEXGB_CNN_MMA the mma.sync
+ * kernel; LEXGB_CNN_TCGEN05 the
+ * tcgen05 kernel only (a grid it does not fit is an error).  Set it before capturing a step graph.
+ * lexgb_cnn_take_timeouts: the number of bounded waits of the tcgen05 kernel that gave up since
+ * the last call (0 in normal operation; such a tile's outputs are not written), then reset. */
+enum { LEXGB_CNN_AUTO = 0, LEXGB_CNN_MMA = 1, LEXGB_CNN_TCGEN05 = 2 };
+int lexgb_cnn_set_kernel(int which);
+int lexgb_cnn_take_timeouts(unsigned int *n);
 int lexgb_cnn_gelu_bwd(long long npts, int c, int cpad, const float *dy, const float *pre, void *g_bf16,
                        void *stream);
 int lexgb_cnn_conv3d_dw(int nx, int ny, int nz, int cin, int cout, int gstride, const void *x, const void *g,

@@ -67,6 +67,8 @@ SIGNATURES = {
     "lexgb_step_vjp_kept": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), _I]),
     "lexgb_cnn_conv3d": (_I, [_I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _I, _I, _P]),
     "lexgb_cnn_gelu_bwd": (_I, [ctypes.c_longlong, _I, _I, _P, _P, _P, _P]),
+    "lexgb_cnn_set_kernel": (_I, [_I]),
+    "lexgb_cnn_take_timeouts": (_I, [_P]),
     "lexgb_cnn_conv3d_dw": (_I, [_I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P]),
     "lexgb_cnn_adam": (_I, [ctypes.c_longlong, _P, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                             ctypes.c_float, _I, _P]),

@@ -501,9 +501,20 @@ cudaError_t launch_conv_smem(int nx, int ny, int nz, const __nv_bfloat16* x, con
                             pdl ? 1 : 0);
 }
 
+// which convolution kernel launch_cnn_conv3d uses (LEXGB_CNN_AUTO: tcgen05 where the grid fits its
+// 8 x 16 tiles and has at least kConvTcMinPoints points, else mma.sync); process-wide, set by
+// lexgb_cnn_set_kernel
+int g_conv_kernel = LEXGB_CNN_AUTO;
+constexpr long long kConvTcMinPoints = 1ll << 18;   // below: too few tiles for the tcgen05 pipeline
+
 cudaError_t launch_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const void* x, const void* w,
                               const float* bias, float* pre, void* ybf, float* yf, int gelu, int creal,
                               cudaStream_t st, bool pdl) {
+  const bool big = (long long)nx * ny * nz >= kConvTcMinPoints;
+  if (conv_tc_fits(nx, ny, nz, cin, cout, x) &&
+      (g_conv_kernel == LEXGB_CNN_TCGEN05 || (g_conv_kernel == LEXGB_CNN_AUTO && big)))
+    return launch_conv_tc(nx, ny, nz, cin, cout, x, w, bias, pre, ybf, yf, gelu, creal, st, pdl);
+  if (g_conv_kernel == LEXGB_CNN_TCGEN05) return cudaErrorInvalidValue;
   if (!(cin == 16 || cin == 32) || !(cout == 8 || cout == 16 || cout == 32) || nx % 16) return cudaErrorInvalidValue;
   const __nv_bfloat16* xb = (const __nv_bfloat16*)x;
   const __nv_bfloat16* wb = (const __nv_bfloat16*)w;
@@ -517,6 +528,7 @@ cudaError_t launch_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const v
 cudaError_t conv_prepare() {
   int cap;
   cudaError_t e;
+  if ((e = conv_tc_prepare()) != cudaSuccess) return e;
   if ((e = conv_grid<16, 8>(&cap)) != cudaSuccess) return e;
   if ((e = conv_grid<16, 16>(&cap)) != cudaSuccess) return e;
   if ((e = conv_grid<16, 32>(&cap)) != cudaSuccess) return e;
@@ -593,6 +605,20 @@ extern "C" int lexgb_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const
   else
     k_conv3d<4><<<blocks, 128, 0, st>>>(nx, ny, nz, cin, xb, wb, bias, pre, yb, y_f32, gelu, creal);
   return cnn_status(cudaGetLastError(), "lexgb_cnn_conv3d");
+}
+
+extern "C" int lexgb_cnn_set_kernel(int which) {
+  using namespace lexgb;
+  if (which != LEXGB_CNN_AUTO && which != LEXGB_CNN_MMA && which != LEXGB_CNN_TCGEN05)
+    return cnn_arg("lexgb_cnn_set_kernel: unknown kernel");
+  g_conv_kernel = which;
+  return LEXGB_OK;
+}
+
+extern "C" int lexgb_cnn_take_timeouts(unsigned int* n) {
+  using namespace lexgb;
+  if (!n) return cnn_arg("lexgb_cnn_take_timeouts: null output");
+  return cnn_status(conv_tc_take_timeouts(n), "lexgb_cnn_take_timeouts");
 }
 
 extern "C" int lexgb_cnn_gelu_bwd(long long npts, int c, int cpad, const float* dy, const float* pre, void* g_bf16,

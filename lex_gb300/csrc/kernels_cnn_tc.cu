@@ -1,0 +1,447 @@
+// kernels_cnn_tc.cu - the learned SGS correction's 3x3x3 convolution on the 5th-generation tensor
+// cores (tcgen05.mma, accumulators in tensor memory), as an implicit GEMM per tile of points:
+//
+//   D[128 points][N] = sum over the 27 offsets and the input channels of
+//                      A[128 points][Cin] (the input shifted by the offset) x B[Cin][N] (the offset's weights)
+//
+// A block owns a column of 8 (x) x 16 (y) points and marches up a chunk of levels, with its warps
+// specialised:
+//   warp 4 (producer)  loads each input plane the chunk needs (10 x 18 points with the one-point
+//                      halo, zero outside the grid by the tensor map's out-of-bounds fill) by TMA
+//                      (cp.async.bulk.tensor, one box per 8-channel group) into a ring of plane
+//                      slots; a slot's full barrier completes on the bytes' arrival;
+//   warp 5 (MMA)       for level z waits for planes z-1, z, z+1 and for a free accumulator, issues
+//                      the 27 x Cin/16 MMAs (M = 128, N = Cout padded to a multiple of 16, K = 16,
+//                      BF16 in, FP32 accumulate) into one of two accumulators, and commits them
+//                      to the accumulator's full barrier and to plane z-1's empty barrier;
+//   warps 0-3          (the four tensor-memory lane quarters) wait for an accumulator, read their
+//                      32 rows (tcgen05.ld), free it, and apply the epilogue of k_conv3d_smem (bias,
+//                      FP32 pre-activation, GELU, padding channels zero, BF16 / FP32 output).
+// Every wait is bounded: one that gives up counts a timeout in g_tc_timeouts and sets the block's
+// abort flag, which ends the other roles' waits; the block then waits (bounded) for the MMAs it
+// issued, frees its tensor memory and returns.
+//
+// Shared-memory layouts (16-byte pieces; the tensor cores' canonical K-major layout without
+// swizzle, core matrix = 8 rows of 16 bytes):
+//   weights  Wsm[27][CIN/8][NP][8]         core matrix = 8 output channels x 8 inputs; K step
+//                                          NP x 16 B (LBO), next 8 output channels 128 B (SBO)
+//   planes   Psm[R][CIN/8][18][10][8]      slot, channel group (its box padded to 128-byte
+//                                          alignment), row, x; core matrix = 8 consecutive x
+//                                          points; K step = the next channel group's box (LBO),
+//                                          next row of the tile 160 B (SBO)
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "lexgb_cnn.cuh"
+
+namespace lexgb {
+
+__device__ unsigned int g_tc_timeouts = 0;   // bounded waits of k_conv3d_tc that gave up
+
+namespace {
+
+constexpr int TC_TX = 8, TC_TY = 16, TC_HX = TC_TX + 2, TC_HY = TC_TY + 2;
+constexpr int TC_THREADS = 192;               // 4 epilogue warps, the producer, the MMA warp
+constexpr int TC_TMEM_COLS = 128;             // allocated columns (2 accumulators of N <= 32)
+constexpr long long TC_POLLS = 1ll << 24;     // mbarrier polls before a wait gives up
+constexpr int TC_BOX_BYTES = TC_HY * TC_HX * 16;                  // one channel group's box: 2880
+constexpr int TC_GROUP_BYTES = (TC_BOX_BYTES + 127) / 128 * 128;  // padded to 128 bytes: 2944
+
+template <int CIN, int COUT>
+struct TcLayout {
+  static constexpr int NP = COUT < 16 ? 16 : COUT;  // N of the MMA (a multiple of 16 for M = 128)
+  static constexpr int CG = CIN / 8;                // channel groups of 8 (16 bytes)
+  static constexpr int R = CIN == 32 ? 4 : 6;       // plane slots (two blocks per SM fit)
+  static constexpr int W_BYTES = 27 * CG * NP * 16;
+  static constexpr int PLANE_BYTES = CG * TC_GROUP_BYTES;
+  static constexpr int P_BYTES = R * PLANE_BYTES;
+  static constexpr int A_LBO = TC_GROUP_BYTES;      // next channel group
+  static constexpr int A_SBO = TC_HX * 16;          // next row of the tile (8 points on)
+  static constexpr int B_LBO = NP * 16;             // next input-channel group
+  static constexpr int B_SBO = 128;                 // next 8 output channels
+  static constexpr int BAR_BYTES = (2 * R + 4) * 8 + 16;
+  // + alignment slack, barriers, tensor-memory address, abort flag, bias
+  static constexpr size_t BYTES = 128 + (size_t)W_BYTES + P_BYTES + BAR_BYTES + NP * 4;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void cp16(uint32_t dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0));
+}
+
+// canonical K-major, no-swizzle shared-memory matrix descriptor
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= 1ull << 46;  // descriptor version
+  return d;         // base offset 0, swizzle none
+}
+
+// instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, M x N
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16_tc(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// Bounded wait for phase `parity` of an mbarrier; gives up early when the block's abort flag is set.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const volatile int* abort) {
+  for (long long i = 0; i < TC_POLLS; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((i & 1023) == 1023 && *abort) return false;
+  }
+  return false;
+}
+
+// a 4-D box (channel, x, y, z) of a tensor map into shared memory, completing on an mbarrier
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c, int x, int y, int z,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+      "%5}], [%6];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ float gelu_fast(float x) {
+  const float k0 = 0.7978845608028654f;  // sqrt(2/pi)
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(k0 * (x + 0.044715f * x * x * x)));
+  return 0.5f * x * (1.f + t);
+}
+
+__device__ __forceinline__ void tmem_load16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(TC_THREADS) k_conv3d_tc(const __grid_constant__ CUtensorMap xmap, int nx, int ny,
+                                                          int nz, int zc, const __nv_bfloat16* __restrict__ w,
+                                                          const float* __restrict__ bias, float* __restrict__ pre,
+                                                          __nv_bfloat16* __restrict__ ybf, float* __restrict__ yf,
+                                                          int gelu, int creal, int early_weights) {
+  using L = TcLayout<CIN, COUT>;
+  constexpr int NP = L::NP, CG = L::CG, R = L::R;
+  extern __shared__ unsigned char tc_raw[];
+  const uint32_t raw_s = smem_u32(tc_raw);
+  unsigned char* smem = tc_raw + ((128u - (raw_s & 127u)) & 127u);   // 128-byte aligned for TMA
+  const uint32_t w_s = smem_u32(smem), p_s = w_s + L::W_BYTES, bar_s = p_s + L::P_BYTES;
+  // barriers: full[R], empty[R], acc_full[2], acc_empty[2]; then the tensor-memory address and abort flag
+  auto full = [&](int s) { return bar_s + 8u * s; };
+  auto empty = [&](int s) { return bar_s + 8u * (R + s); };
+  auto acc_full = [&](int a) { return bar_s + 8u * (2 * R + a); };
+  auto acc_empty = [&](int a) { return bar_s + 8u * (2 * R + 2 + a); };
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + L::W_BYTES + L::P_BYTES + (2 * R + 4) * 8);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
+  float* bsm = reinterpret_cast<float*>(smem + L::W_BYTES + L::P_BYTES + L::BAR_BYTES);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 5) {  // tensor memory for the two accumulators
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < R; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(empty(s), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(acc_full(a), 1);
+      mbar_init(acc_empty(a), 4);
+    }
+    *abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // weights Wsm[tap][cg][n][8] from w[tap][COUT][CIN] (rows n >= COUT zero) and the bias, by cp.async
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if (!early_weights) asm volatile("griddepcontrol.wait;" ::: "memory");
+  for (int e = tid; e < 27 * CG * NP; e += TC_THREADS) {
+    const int n = e % NP, cg = (e / NP) % CG, tap = e / (NP * CG);
+    const bool ok = n < COUT;
+    cp16(w_s + (uint32_t)e * 16u, w + ((long long)(tap * COUT + (ok ? n : 0)) * CIN + cg * 8), ok);
+  }
+  if (tid < NP) bsm[tid] = (bias && tid < COUT) ? bias[tid] : 0.f;
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // weights -> the tensor cores
+  if (early_weights) asm volatile("griddepcontrol.wait;" ::: "memory");   // the input is ready
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  const int tiles_x = nx / TC_TX, tiles_y = ny / TC_TY;
+  const int tx = blockIdx.x % tiles_x, ty = (blockIdx.x / tiles_x) % tiles_y, ch = blockIdx.x / (tiles_x * tiles_y);
+  const int x0 = tx * TC_TX, y0 = ty * TC_TY, z0 = ch * zc, z1 = min(z0 + zc, nz);
+  const int p0 = z0 - 1;   // first plane of the chunk; plane p uses slot (p - p0) % R, fill (p - p0) / R
+
+  if (warp == 4) {
+    // ---------------- producer: planes z0-1 .. z1 ----------------
+    if (lane == 0) {
+      for (int p = p0; p <= z1; ++p) {
+        const int s = (p - p0) % R, k = (p - p0) / R;
+        if (k > 0 && !mbar_wait(empty(s), (k - 1) & 1, abort)) {
+          atomicAdd(&g_tc_timeouts, 1u);
+          *abort = 1;
+          break;
+        }
+        mbar_expect_tx(full(s), CG * TC_BOX_BYTES);
+        for (int cg = 0; cg < CG; ++cg)
+          tma_load_4d(p_s + s * L::PLANE_BYTES + cg * TC_GROUP_BYTES, &xmap, cg * 8, x0 - 1, y0 - 1, p, full(s));
+      }
+    }
+  } else if (warp == 5) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc_idesc(128, NP);
+      bool ok = true;
+      int issued = 0;
+      for (int z = z0; z < z1 && ok; ++z) {
+        const int i = z - z0, a = i & 1;
+        // planes z-1, z (already complete after the first level) and z+1
+        for (int p = (z == z0 ? z - 1 : z + 1); p <= z + 1 && ok; ++p) {
+          const int s = (p - p0) % R, k = (p - p0) / R;
+          ok = mbar_wait(full(s), k & 1, abort);
+        }
+        if (ok && i >= 2) ok = mbar_wait(acc_empty(a), ((i >> 1) - 1) & 1, abort);
+        if (!ok) {
+          atomicAdd(&g_tc_timeouts, 1u);
+          *abort = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        uint32_t acc = 0;
+#pragma unroll
+        for (int dz = 0; dz < 3; ++dz) {
+          const uint32_t plane = p_s + ((z - 1 + dz - p0) % R) * L::PLANE_BYTES;
+          const uint64_t a0 = smem_desc(plane, L::A_LBO, L::A_SBO);
+#pragma unroll
+          for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+            for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+              for (int ks = 0; ks < CIN / 16; ++ks) {
+                const int tap = dz * 9 + dy * 3 + dx;
+                // the start address is the descriptor's low field (16-byte units): add the offset
+                const uint64_t ad = a0 + (uint64_t)((2 * ks * TC_GROUP_BYTES + (dy * TC_HX + dx) * 16) >> 4);
+                const uint64_t bd = smem_desc(w_s + (uint32_t)((tap * CG + 2 * ks) * NP * 16), L::B_LBO, L::B_SBO);
+                mma_bf16_tc(tmem + (uint32_t)(a * NP), ad, bd, idesc, acc);
+                acc = 1;
+              }
+        }
+        mma_commit(acc_full(a));
+        mma_commit(empty((z - 1 - p0) % R));   // plane z-1 is not read again
+        ++issued;
+      }
+      if (!ok && issued > 0) {  // the last commit before the abort: a bounded wait before the memory goes
+        const int i = issued - 1;
+        mbar_wait(acc_full(i & 1), (i >> 1) & 1, abort);
+      }
+    }
+  } else {
+    // ---------------- epilogue: warps 0-3, tensor-memory lanes 32 warp .. 32 warp + 31 ----------------
+    const int r = 32 * warp + lane;   // row r <-> point (x0 + r % 8, y0 + r / 8)
+    for (int z = z0; z < z1; ++z) {
+      const int i = z - z0, a = i & 1;
+      if (!__all_sync(0xffffffffu, mbar_wait(acc_full(a), (i >> 1) & 1, abort))) {   // warp-uniform
+        if (lane == 0) {
+          atomicAdd(&g_tc_timeouts, 1u);
+          *abort = 1;
+        }
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      float v[NP];
+#pragma unroll
+      for (int c = 0; c < NP; c += 16) tmem_load16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(a * NP + c), v + c);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_empty(a));   // the accumulator may be overwritten
+      const long long p = ((long long)z * ny + y0 + r / TC_TX) * nx + x0 + r % TC_TX;
+#pragma unroll
+      for (int co = 0; co < COUT; co += 2) {
+        float v0 = v[co] + bsm[co], v1 = v[co + 1] + bsm[co + 1];
+        if (pre) *reinterpret_cast<float2*>(pre + p * COUT + co) = make_float2(v0, v1);
+        if (gelu) {
+          v0 = gelu_fast(v0);
+          v1 = gelu_fast(v1);
+        }
+        if (co >= creal) v0 = 0.f;
+        if (co + 1 >= creal) v1 = 0.f;
+        if (ybf) *reinterpret_cast<__nv_bfloat162*>(ybf + p * COUT + co) = __floats2bfloat162_rn(v0, v1);
+        if (yf) *reinterpret_cast<float2*>(yf + p * COUT + co) = make_float2(v0, v1);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 5) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+  }
+}
+
+constexpr int TC_MAX_DEVICES = 64;
+
+template <int CIN, int COUT>
+cudaError_t tc_grid(int* cap) {
+  static int grid_cap[TC_MAX_DEVICES] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= TC_MAX_DEVICES) return cudaErrorInvalidDevice;
+  if (!grid_cap[dev]) {
+    using L = TcLayout<CIN, COUT>;
+    e = cudaFuncSetAttribute(k_conv3d_tc<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_conv3d_tc<CIN, COUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    int sms = 0, per = 0;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv3d_tc<CIN, COUT>, TC_THREADS, L::BYTES)) !=
+        cudaSuccess)
+      return e;
+    grid_cap[dev] = sms * (per < 1 ? 1 : per);
+  }
+  *cap = grid_cap[dev];
+  return cudaSuccess;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn tc_encoder() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// activations [z][y][x][cin] BF16 as a 4-D tensor (channel, x, y, z); box = one 8-channel group of
+// a 10 x 18 plane with halo; out-of-bounds elements read as zero
+bool make_xmap(CUtensorMap* map, const void* x, int nx, int ny, int nz, int cin) {
+  EncodeTiledFn enc = tc_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)nx * cin * 2, (cuuint64_t)ny * nx * cin * 2};
+  const cuuint32_t box[4] = {8, TC_HX, TC_HY, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int CIN, int COUT>
+cudaError_t launch_tc(int nx, int ny, int nz, const void* x, const __nv_bfloat16* w, const float* bias, float* pre,
+                      __nv_bfloat16* ybf, float* yf, int gelu, int creal, cudaStream_t st, bool pdl) {
+  int cap = 0;
+  cudaError_t e = tc_grid<CIN, COUT>(&cap);
+  if (e != cudaSuccess) return e;
+  CUtensorMap xmap;
+  if (!make_xmap(&xmap, x, nx, ny, nz, CIN)) return cudaErrorInvalidValue;
+  // level chunks: enough blocks for about two waves of resident blocks, chunks of at least 4 levels
+  const int tiles = (nx / TC_TX) * (ny / TC_TY);
+  int nch = (2 * cap + tiles - 1) / tiles;
+  nch = nch < 1 ? 1 : (nch > (nz + 3) / 4 ? (nz + 3) / 4 : nch);
+  const int zc = (nz + nch - 1) / nch;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(tiles * ((nz + zc - 1) / zc)));
+  cfg.blockDim = dim3(TC_THREADS);
+  cfg.dynamicSmemBytes = TcLayout<CIN, COUT>::BYTES;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k_conv3d_tc<CIN, COUT>, xmap, nx, ny, nz, zc, w, bias, pre, ybf, yf, gelu, creal,
+                            pdl ? 1 : 0);
+}
+
+}  // namespace
+
+bool conv_tc_fits(int nx, int ny, int nz, int cin, int cout, const void* x) {
+  return (cin == 16 || cin == 32) && (cout == 8 || cout == 16 || cout == 32) && nx > 0 && ny > 0 && nz > 0 &&
+         nx % TC_TX == 0 && ny % TC_TY == 0 && ((uintptr_t)x & 15) == 0 && tc_encoder() != nullptr;
+}
+
+cudaError_t launch_conv_tc(int nx, int ny, int nz, int cin, int cout, const void* x, const void* w, const float* bias,
+                           float* pre, void* ybf, float* yf, int gelu, int creal, cudaStream_t st, bool pdl) {
+  if (!conv_tc_fits(nx, ny, nz, cin, cout, x)) return cudaErrorInvalidValue;
+  const __nv_bfloat16* wb = (const __nv_bfloat16*)w;
+  __nv_bfloat16* yb = (__nv_bfloat16*)ybf;
+#define LEXGB_TC(CI, CO) launch_tc<CI, CO>(nx, ny, nz, x, wb, bias, pre, yb, yf, gelu, creal, st, pdl)
+  if (cin == 16) return cout == 8 ? LEXGB_TC(16, 8) : cout == 16 ? LEXGB_TC(16, 16) : LEXGB_TC(16, 32);
+  return cout == 8 ? LEXGB_TC(32, 8) : cout == 16 ? LEXGB_TC(32, 16) : LEXGB_TC(32, 32);
+#undef LEXGB_TC
+}
+
+cudaError_t conv_tc_prepare() {
+  int cap;
+  cudaError_t e;
+  if ((e = tc_grid<16, 8>(&cap)) != cudaSuccess) return e;
+  if ((e = tc_grid<16, 16>(&cap)) != cudaSuccess) return e;
+  if ((e = tc_grid<16, 32>(&cap)) != cudaSuccess) return e;
+  if ((e = tc_grid<32, 8>(&cap)) != cudaSuccess) return e;
+  if ((e = tc_grid<32, 16>(&cap)) != cudaSuccess) return e;
+  return tc_grid<32, 32>(&cap);
+}
+
+cudaError_t conv_tc_take_timeouts(unsigned int* n) {
+  unsigned int zero = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(n, g_tc_timeouts, sizeof(unsigned int));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyToSymbol(g_tc_timeouts, &zero, sizeof(unsigned int));
+}
+
+}  // namespace lexgb

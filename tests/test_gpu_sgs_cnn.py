@@ -35,10 +35,32 @@ def _rel(a, b):
     return float((a - b).norm() / b.norm())
 
 
-def test_cnn_forward_and_gradients_match_torch(built_lib):
+@pytest.fixture
+def conv_kernel(built_lib):
+    """Select the convolution kernel for one test (lexgb_cnn_set_kernel), back to AUTO after it;
+    a tcgen05 test also checks that none of its bounded waits gave up."""
+    import ctypes
+    chosen = {}
+
+    def use(name):
+        chosen["name"] = name
+        code = {"auto": 0, "mma": 1, "tcgen05": 2}[name]
+        assert built_lib.lexgb_cnn_set_kernel(code) == 0
+    yield use
+    n = ctypes.c_uint(0)
+    assert built_lib.lexgb_cnn_take_timeouts(ctypes.byref(n)) == 0
+    built_lib.lexgb_cnn_set_kernel(0)
+    assert n.value == 0, n.value
+
+
+KERNEL_CASES = [("mma", (16, 8, 6)), ("tcgen05", (16, 16, 6)), ("tcgen05", (32, 32, 8))]
+
+
+@pytest.mark.parametrize("kernel,dims", KERNEL_CASES, ids=["%s-%dx%dx%d" % ((k,) + d) for k, d in KERNEL_CASES])
+def test_cnn_forward_and_gradients_match_torch(conv_kernel, kernel, dims):
     torch = pytest.importorskip("torch")
     from lex_gb300 import sgs_cnn
-    dims = (16, 8, 6)
+    conv_kernel(kernel)
     n = dims[0] * dims[1] * dims[2]
     net = sgs_cnn.SGSNet(seed=1, init_scale=1.0, zero_last=False)
     for t in net.params():
@@ -76,3 +98,38 @@ def test_adam_matches_formula(built_lib):
             w0[i] = w0[i] - lr * (m[i] / (1 - b1 ** step)) / ((v[i] / (1 - b2 ** step)).sqrt() + eps)
     for a, b in zip(net.params(), w0):
         assert float((a - b).abs().max()) < 1e-6
+
+
+@pytest.mark.parametrize("cin,cout", [(16, 32), (32, 32), (32, 8), (16, 8)])
+def test_tcgen05_convolution_matches_mma_sync(conv_kernel, cin, cout):
+    """One convolution layer (zero padding, bias, FP32 pre-activation) on the tcgen05 kernel against
+    the mma.sync kernel on the same BF16 inputs: both accumulate the same BF16 products in FP32, in a
+    different order, so they agree to FP32 summation rounding."""
+    torch = pytest.importorskip("torch")
+    nx, ny, nz = 32, 16, 5
+    g = torch.Generator(device="cpu").manual_seed(cin + cout)
+    x = torch.randn(nz * ny * nx, cin, generator=g).to(torch.bfloat16).cuda()
+    w = (0.2 * torch.randn(27, cout, cin, generator=g)).to(torch.bfloat16).cuda()
+    b = torch.randn(cout, generator=g).cuda()
+    outs = {}
+    for kernel in ("mma", "tcgen05"):
+        conv_kernel(kernel)
+        pre = torch.empty(nz * ny * nx, cout, device="cuda")
+        yb = torch.empty(nz * ny * nx, cout, dtype=torch.bfloat16, device="cuda")
+        rc = _conv_call(nx, ny, nz, cin, cout, x, w, b, pre, yb)
+        assert rc == 0
+        torch.cuda.synchronize()
+        outs[kernel] = (pre, yb)
+    a, r = outs["tcgen05"][0], outs["mma"][0]
+    assert _rel(a, r) < 1e-5, _rel(a, r)
+    assert _rel(outs["tcgen05"][1].float()[:, :5], outs["mma"][1].float()[:, :5]) < 1e-2
+
+
+def _conv_call(nx, ny, nz, cin, cout, x, w, b, pre, yb):
+    """lexgb_cnn_conv3d with GELU, 5 real output channels, the default stream."""
+    import ctypes
+    from lex_gb300 import _lib
+    lib = _lib.load()
+    return lib.lexgb_cnn_conv3d(nx, ny, nz, cin, cout, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(w.data_ptr()),
+                                ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(pre.data_ptr()),
+                                ctypes.c_void_p(yb.data_ptr()), None, 1, 5, None)
