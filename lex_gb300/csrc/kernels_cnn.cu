@@ -511,7 +511,7 @@ cudaError_t launch_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const v
                               const float* bias, float* pre, void* ybf, float* yf, int gelu, int creal,
                               cudaStream_t st, bool pdl) {
   const bool big = (long long)nx * ny * nz >= kConvTcMinPoints;
-  if (conv_tc_fits(nx, ny, nz, cin, cout, x) &&
+  if (conv_tc_fits(nx, ny, nz, cin, cout, x, pre, ybf, yf) &&
       (g_conv_kernel == LEXGB_CNN_TCGEN05 || (g_conv_kernel == LEXGB_CNN_AUTO && big)))
     return launch_conv_tc(nx, ny, nz, cin, cout, x, w, bias, pre, ybf, yf, gelu, creal, st, pdl);
   if (g_conv_kernel == LEXGB_CNN_TCGEN05) return cudaErrorInvalidValue;

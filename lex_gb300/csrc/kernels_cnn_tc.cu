@@ -231,6 +231,9 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3d_tc(const __grid_constant_
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       constexpr uint32_t idesc = tc_idesc(128, NP);
+      // descriptors: the start address is the low field (16-byte units), so an operand at a fixed
+      // offset from a base is the base's descriptor plus the offset / 16
+      const uint64_t b0 = smem_desc(w_s, L::B_LBO, L::B_SBO);
       bool ok = true;
       int issued = 0;
       for (int z = z0; z < z1 && ok; ++z) {
@@ -259,9 +262,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3d_tc(const __grid_constant_
 #pragma unroll
               for (int ks = 0; ks < CIN / 16; ++ks) {
                 const int tap = dz * 9 + dy * 3 + dx;
-                // the start address is the descriptor's low field (16-byte units): add the offset
                 const uint64_t ad = a0 + (uint64_t)((2 * ks * TC_GROUP_BYTES + (dy * TC_HX + dx) * 16) >> 4);
-                const uint64_t bd = smem_desc(w_s + (uint32_t)((tap * CG + 2 * ks) * NP * 16), L::B_LBO, L::B_SBO);
+                const uint64_t bd = b0 + (uint64_t)(((tap * CG + 2 * ks) * NP * 16) >> 4);
                 mma_bf16_tc(tmem + (uint32_t)(a * NP), ad, bd, idesc, acc);
                 acc = 1;
               }
@@ -295,19 +297,39 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3d_tc(const __grid_constant_
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(acc_empty(a));   // the accumulator may be overwritten
+      // the point's COUT channels as 16-byte stores (COUT x 2 bytes BF16, COUT x 4 bytes FP32)
       const long long p = ((long long)z * ny + y0 + r / TC_TX) * nx + x0 + r % TC_TX;
 #pragma unroll
-      for (int co = 0; co < COUT; co += 2) {
-        float v0 = v[co] + bsm[co], v1 = v[co + 1] + bsm[co + 1];
-        if (pre) *reinterpret_cast<float2*>(pre + p * COUT + co) = make_float2(v0, v1);
-        if (gelu) {
-          v0 = gelu_fast(v0);
-          v1 = gelu_fast(v1);
+      for (int co = 0; co < COUT; ++co) v[co] += bsm[co];
+      if (pre) {
+#pragma unroll
+        for (int co = 0; co < COUT; co += 4)
+          *reinterpret_cast<float4*>(pre + p * COUT + co) = make_float4(v[co], v[co + 1], v[co + 2], v[co + 3]);
+      }
+#pragma unroll
+      for (int co = 0; co < COUT; ++co) {
+        const float t = gelu ? gelu_fast(v[co]) : v[co];
+        v[co] = co < creal ? t : 0.f;
+      }
+      if (ybf) {
+#pragma unroll
+        for (int co = 0; co < COUT; co += 8) {
+          uint4 q;
+          __nv_bfloat162 h0 = __floats2bfloat162_rn(v[co], v[co + 1]);
+          __nv_bfloat162 h1 = __floats2bfloat162_rn(v[co + 2], v[co + 3]);
+          __nv_bfloat162 h2 = __floats2bfloat162_rn(v[co + 4], v[co + 5]);
+          __nv_bfloat162 h3 = __floats2bfloat162_rn(v[co + 6], v[co + 7]);
+          q.x = *reinterpret_cast<uint32_t*>(&h0);
+          q.y = *reinterpret_cast<uint32_t*>(&h1);
+          q.z = *reinterpret_cast<uint32_t*>(&h2);
+          q.w = *reinterpret_cast<uint32_t*>(&h3);
+          *reinterpret_cast<uint4*>(ybf + p * COUT + co) = q;
         }
-        if (co >= creal) v0 = 0.f;
-        if (co + 1 >= creal) v1 = 0.f;
-        if (ybf) *reinterpret_cast<__nv_bfloat162*>(ybf + p * COUT + co) = __floats2bfloat162_rn(v0, v1);
-        if (yf) *reinterpret_cast<float2*>(yf + p * COUT + co) = make_float2(v0, v1);
+      }
+      if (yf) {
+#pragma unroll
+        for (int co = 0; co < COUT; co += 4)
+          *reinterpret_cast<float4*>(yf + p * COUT + co) = make_float4(v[co], v[co + 1], v[co + 2], v[co + 3]);
       }
     }
   }
@@ -389,11 +411,19 @@ cudaError_t launch_tc(int nx, int ny, int nz, const void* x, const __nv_bfloat16
   if (e != cudaSuccess) return e;
   CUtensorMap xmap;
   if (!make_xmap(&xmap, x, nx, ny, nz, CIN)) return cudaErrorInvalidValue;
-  // level chunks: enough blocks for about two waves of resident blocks, chunks of at least 4 levels
+  // level chunks of at least 4 levels: the count whose blocks fill their waves of resident blocks
+  // best (ties: fewer chunks, since every chunk stages the weights and two extra planes)
   const int tiles = (nx / TC_TX) * (ny / TC_TY);
-  int nch = (2 * cap + tiles - 1) / tiles;
-  nch = nch < 1 ? 1 : (nch > (nz + 3) / 4 ? (nz + 3) / 4 : nch);
-  const int zc = (nz + nch - 1) / nch;
+  int zc = nz;
+  double best = -1.0;
+  for (int nch = 1; nch <= (nz + 3) / 4; ++nch) {
+    const int z = (nz + nch - 1) / nch, blocks = tiles * ((nz + z - 1) / z);
+    const double fill = (double)blocks / ((double)((blocks + cap - 1) / cap) * cap);
+    if (fill > best + 1e-9) {
+      best = fill;
+      zc = z;
+    }
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(tiles * ((nz + zc - 1) / zc)));
   cfg.blockDim = dim3(TC_THREADS);
@@ -410,14 +440,16 @@ cudaError_t launch_tc(int nx, int ny, int nz, const void* x, const __nv_bfloat16
 
 }  // namespace
 
-bool conv_tc_fits(int nx, int ny, int nz, int cin, int cout, const void* x) {
+bool conv_tc_fits(int nx, int ny, int nz, int cin, int cout, const void* x, const void* pre, const void* ybf,
+                  const void* yf) {
+  const uintptr_t align = (uintptr_t)x | (uintptr_t)pre | (uintptr_t)ybf | (uintptr_t)yf;   // 16-byte TMA / stores
   return (cin == 16 || cin == 32) && (cout == 8 || cout == 16 || cout == 32) && nx > 0 && ny > 0 && nz > 0 &&
-         nx % TC_TX == 0 && ny % TC_TY == 0 && ((uintptr_t)x & 15) == 0 && tc_encoder() != nullptr;
+         nx % TC_TX == 0 && ny % TC_TY == 0 && (align & 15) == 0 && tc_encoder() != nullptr;
 }
 
 cudaError_t launch_conv_tc(int nx, int ny, int nz, int cin, int cout, const void* x, const void* w, const float* bias,
                            float* pre, void* ybf, float* yf, int gelu, int creal, cudaStream_t st, bool pdl) {
-  if (!conv_tc_fits(nx, ny, nz, cin, cout, x)) return cudaErrorInvalidValue;
+  if (!conv_tc_fits(nx, ny, nz, cin, cout, x, pre, ybf, yf)) return cudaErrorInvalidValue;
   const __nv_bfloat16* wb = (const __nv_bfloat16*)w;
   __nv_bfloat16* yb = (__nv_bfloat16*)ybf;
 #define LEXGB_TC(CI, CO) launch_tc<CI, CO>(nx, ny, nz, x, wb, bias, pre, yb, yf, gelu, creal, st, pdl)

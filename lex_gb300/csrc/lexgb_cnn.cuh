@@ -8,7 +8,8 @@
 
 namespace lexgb {
 // tcgen05 convolution (kernels_cnn_tc.cu): shape rule, launch, one-time set-up, timeout count
-bool conv_tc_fits(int nx, int ny, int nz, int cin, int cout, const void* x);
+bool conv_tc_fits(int nx, int ny, int nz, int cin, int cout, const void* x, const void* pre, const void* ybf,
+                  const void* yf);
 cudaError_t launch_conv_tc(int nx, int ny, int nz, int cin, int cout, const void* x, const void* w, const float* bias,
                            float* pre, void* ybf, float* yf, int gelu, int creal, cudaStream_t st, bool pdl);
 cudaError_t conv_tc_prepare();
