@@ -366,7 +366,7 @@ int build_table(lexgb_ctx* c) {
                           c->base64 + 3 * S, c->tab, c->stream));
   float* t = c->tab;
   c->cols = Cols{t,         t + S,     t + 2 * S, t + 3 * S, t + 4 * S,  t + 5 * S,
-                 t + 6 * S, t + 7 * S, t + 8 * S, t + 9 * S, t + 10 * S, t + 11 * S};
+                 t + 6 * S, t + 7 * S, t + 8 * S, t + 9 * S, t + 10 * S, t + 11 * S, t + 12 * S};
   c->base_set = true;
   c->adj_kept = false;
   drop_graph(c);

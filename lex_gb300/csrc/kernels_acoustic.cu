@@ -77,7 +77,7 @@ __device__ __forceinline__ float adv_pi(const Dims& d, const Phys& ph, const Col
   const float wzb = (k == 0) ? 0.f : wb * (c.dpi0dz[k] + (p0 - LD(ps, d.at(i, j, k - 1))) * ph.rdz);
   const float wzt = (k + 1 >= d.nz) ? 0.f : wt * (c.dpi0dz[k + 1] + (LD(ps, d.at(i, j, k + 1)) - p0) * ph.rdz);
   return -(0.5f * (ue * gxe + uw * gxw) + 0.5f * (vn * gyn + vs * gys) +
-           (0.5f * wzb * c.rho_face[k] + 0.5f * wzt * c.rho_face[k + 1]) / c.rho[k]);
+           (0.5f * wzb * c.rho_face[k] + 0.5f * wzt * c.rho_face[k + 1]) * c.rho_inv[k]);
 }
 
 __global__ void __launch_bounds__(BX* BY* BZ) k_acoustic(Dims d, Phys ph, Cols c, AcousticIn a, AcousticOut o,
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(256) k_acoustic_vec(Dims d, Phys ph, Cols c, A
   sc[V + 1] = sE;
 #pragma unroll
   for (int l = 0; l < V; ++l) sc[l + 1] = S0[l];
-  const float rho = c.rho[k], rfb = c.rho_face[k], rft = c.rho_face[k + 1];
+  const float rho = c.rho[k], rhoi = c.rho_inv[k], rfb = c.rho_face[k], rft = c.rho_face[k + 1];
   const float dzb = c.dpi0dz[k], dzt = c.dpi0dz[k + 1], pi0 = c.pi0[k];
   float outp[V], outv[V], outw[V], outu[V];
 #pragma unroll
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(256) k_acoustic_vec(Dims d, Phys ph, Cols c, A
     const float wzb = has_b ? wb * (dzb + (s0 - SB[l]) * ph.rdz) : 0.f;
     const float wzt = has_t ? wt * (dzt + (ST[l] - s0) * ph.rdz) : 0.f;
     const float ap = -(0.5f * (un[l + 1] * gxe + un[l] * gxw) + 0.5f * (vn * gyn + vs * gys) +
-                       (0.5f * wzb * rfb + 0.5f * wzt * rft) / rho);
+                       (0.5f * wzb * rfb + 0.5f * wzt * rft) * rhoi);
     const float dpdt = -kRdCv * ((pi0 + s0) * div) + ap;
     outp[l] = p0 + (kDivDamp * dpdt) * dtau;
     outv[l] = vs;
@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(256) k_acoustic_zm(Dims d, Phys ph, Cols c, Ac
     sc[V + 1] = sE;
 #pragma unroll
     for (int l = 0; l < V; ++l) sc[l + 1] = S0[l];
-    const float rho = c.rho[k], rfb = c.rho_face[k], rft = c.rho_face[k + 1];
+    const float rho = c.rho[k], rhoi = c.rho_inv[k], rfb = c.rho_face[k], rft = c.rho_face[k + 1];
     const float dzb = c.dpi0dz[k], dzt = c.dpi0dz[k + 1], pi0 = c.pi0[k];
     float outp[V], outv[V], wt[V];
 #pragma unroll
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(256) k_acoustic_zm(Dims d, Phys ph, Cols c, Ac
       const float wzb = has_b ? wb * (dzb + (s0 - SB[l]) * ph.rdz) : 0.f;
       const float wzt = has_t ? wt[l] * (dzt + (ST[l] - s0) * ph.rdz) : 0.f;
       const float ap = -(0.5f * (un[l + 1] * gxe + un[l] * gxw) + 0.5f * (vn * gyn + vs * gys) +
-                         (0.5f * wzb * rfb + 0.5f * wzt * rft) / rho);
+                         (0.5f * wzb * rfb + 0.5f * wzt * rft) * rhoi);
       const float dpdt = -kRdCv * ((pi0 + s0) * div) + ap;
       outp[l] = p0 + (kDivDamp * dpdt) * dtau;
       outv[l] = vs;
@@ -670,7 +670,7 @@ __global__ void __launch_bounds__(tb::NT, 2) k_acoustic_pair(Dims d, Phys ph, Co
     // ---- Y: sub-step 1 pi' of level n
     if (s1) {
       const bool has_b = n > 0, has_t = n + 1 < nz;
-      const float rho = c.rho[n], rfb = c.rho_face[n], rft = c.rho_face[n + 1];
+      const float rho = c.rho[n], rhoi = c.rho_inv[n], rfb = c.rho_face[n], rft = c.rho_face[n + 1];
       const float dzb = c.dpi0dz[n], dzt = c.dpi0dz[n + 1], pi0 = c.pi0[n];
       auto cell = [&](int cc, int uo, int eo) {
         const float uw = U1c[uo], ue = U1c[uo + 1];
@@ -683,7 +683,7 @@ __global__ void __launch_bounds__(tb::NT, 2) k_acoustic_pair(Dims d, Phys ph, Co
         const float wzb = has_b ? wb * (dzb + (s0 - PSb[cc]) * rdz) : 0.f;
         const float wzt = has_t ? wt * (dzt + (PSu[cc] - s0) * rdz) : 0.f;
         const float ap = -(0.5f * (ue * gxe + uw * gxw) + 0.5f * (vn * gyn + vs * gys) +
-                           (0.5f * wzb * rfb + 0.5f * wzt * rft) / rho);
+                           (0.5f * wzb * rfb + 0.5f * wzt * rft) * rhoi);
         const float dpdt = -kRdCv * ((pi0 + s0) * div) + ap;
         P1c[eo] = P0c[cc] + (kDivDamp * dpdt) * dtau;
       };

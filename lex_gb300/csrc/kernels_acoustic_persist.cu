@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(PNT, 1)
           const float4 wT = !has_t ? zero4() : (kk < SL - 1 ? slot[2 * BOX / 4 + own + PQX * PTY] : wTg);
           float4* pp = &reinterpret_cast<float4*>(sP)[(k * PTY + jj) * PQX + qx];
           const float4 P = *pp;
-          const float rho = c.rho[k], rfb = c.rho_face[k], rft = c.rho_face[k + 1];
+          const float rho = c.rho[k], rhoi = c.rho_inv[k], rfb = c.rho_face[k], rft = c.rho_face[k + 1];
           const float dzb = c.dpi0dz[k], dzt = c.dpi0dz[k + 1], pi0 = c.pi0[k];
           const float un[5] = {UN.x, UN.y, UN.z, UN.w, uE};
           const float sc[6] = {sW, S0.x, S0.y, S0.z, S0.w, sE};
@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(PNT, 1)
             const float wzb = has_b ? wb * (dzb + (s0 - at(SB, l)) * rdz) : 0.f;
             const float wzt = has_t ? wt * (dzt + (at(ST, l) - s0) * rdz) : 0.f;
             const float ap = -(0.5f * (un[l + 1] * gxe + un[l] * gxw) + 0.5f * (vn_ * gyn + vs_ * gys) +
-                               (0.5f * wzb * rfb + 0.5f * wzt * rft) / rho);
+                               (0.5f * wzb * rfb + 0.5f * wzt * rft) * rhoi);
             const float dpdt = -kRdCvP * ((pi0 + s0) * div) + ap;
             outp[l] = at(P, l) + (kDivDamp * dpdt) * dtau;
           }

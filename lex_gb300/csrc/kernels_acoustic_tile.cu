@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(TT, 2) k_acoustic_tile(Dims d, Phys ph, Cols c
     if (!has_t) wt[l] = 0.f;
 
   // ---- new pi' (divergence and advection_pi of the new winds)
-  const float rho = c.rho[k], rfb = c.rho_face[k], rft = c.rho_face[k + 1];
+  const float rho = c.rho[k], rhoi = c.rho_inv[k], rfb = c.rho_face[k], rft = c.rho_face[k + 1];
   const float dzb = c.dpi0dz[k], dzt = c.dpi0dz[k + 1], pi0 = c.pi0[k];
   const float sc[6] = {sW, S0.x, S0.y, S0.z, S0.w, sE};
   float outp[4];
@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(TT, 2) k_acoustic_tile(Dims d, Phys ph, Cols c
     const float wzb = has_b ? wb[l] * (dzb + (s0 - el(SB, l)) * rdz) : 0.f;
     const float wzt = has_t ? wt[l] * (dzt + (el(ST, l) - s0) * rdz) : 0.f;
     const float ap = -(0.5f * (un[l + 1] * gxe + un[l] * gxw) + 0.5f * (vn[l] * gyn + vs[l] * gys) +
-                       (0.5f * wzb * rfb + 0.5f * wzt * rft) / rho);
+                       (0.5f * wzb * rfb + 0.5f * wzt * rft) * rhoi);
     const float dpdt = -kRdCvT * ((pi0 + s0) * div) + ap;
     outp[l] = el(P, l) + (kDivDamp * dpdt) * dtau;
   }

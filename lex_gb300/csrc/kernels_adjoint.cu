@@ -164,8 +164,8 @@ struct AcNbr {
   float unb_w, unb_e, vnb_s, vnb_n, wnb_b, wnb_t;  // adjoints of the output winds on the six faces
   float un_w, un_e, vn_s, vn_n, wn_b, wn_t;        // output winds on the six faces
 };
-struct AcCol {  // column constants of level k
-  float pi0m, pi0, pi0p, rhom, rho, rhop, rfb, rft, dzb, dzt;
+struct AcCol {  // column constants of level k (rho* and their correctly rounded reciprocals *i)
+  float pi0m, pi0, pi0p, rhom, rho, rhop, rhomi, rhoi, rhopi, rfb, rft, dzb, dzt;
   bool hb, ht;
 };
 struct AcOut {
@@ -187,11 +187,11 @@ __device__ __forceinline__ AcOut acoustic_vjp_cell(const AcNbr& n, const AcCol& 
   float Wb = 0.f, Wt = 0.f;
   if (k.hb) {
     const float Z = k.dzb + (s[0] - s[5]) * rdz;
-    Wb = n.wnb_b + (DB - D0) * rdz - 0.5f * Z * k.rfb * (A[0] / k.rho + A[5] / k.rhom);
+    Wb = n.wnb_b + (DB - D0) * rdz - 0.5f * Z * k.rfb * (A[0] * k.rhoi + A[5] * k.rhomi);
   }
   if (k.ht) {
     const float Z = k.dzt + (s[6] - s[0]) * rdz;
-    Wt = n.wnb_t + (D0 - DT) * rdz - 0.5f * Z * k.rft * (A[6] / k.rhop + A[0] / k.rho);
+    Wt = n.wnb_t + (D0 - DT) * rdz - 0.5f * Z * k.rft * (A[6] * k.rhopi + A[0] * k.rhoi);
   }
   AcOut o;
   o.ub = Uw;
@@ -221,12 +221,12 @@ __device__ __forceinline__ AcOut acoustic_vjp_cell(const AcNbr& n, const AcCol& 
   const float wbn = k.hb ? n.wn_b : 0.f, wtn = k.ht ? n.wn_t : 0.f;
   const float div = (ue - uw) * rdx + (vn - vs) * rdy + (wtn - wbn) * rdz;
   const float dap = -(0.5f * (-ue * rdx + uw * rdx) + 0.5f * (-vn * rdy + vs * rdy) +
-                      ((k.hb ? 0.5f * k.rfb * wbn * rdz : 0.f) - (k.ht ? 0.5f * k.rft * wtn * rdz : 0.f)) / k.rho);
+                      ((k.hb ? 0.5f * k.rfb * wbn * rdz : 0.f) - (k.ht ? 0.5f * k.rft * wtn * rdz : 0.f)) * k.rhoi);
   float sb = A[0] * (-kRdCvA * div + dap);
   sb += A[2] * 0.5f * ue * rdx - A[1] * 0.5f * uw * rdx;
   sb += A[4] * 0.5f * vn * rdy - A[3] * 0.5f * vs * rdy;
-  if (k.ht) sb += A[6] * 0.5f * k.rft * wtn * rdz / k.rhop;
-  if (k.hb) sb -= A[5] * 0.5f * k.rfb * wbn * rdz / k.rhom;
+  if (k.ht) sb += A[6] * 0.5f * k.rft * wtn * rdz * k.rhopi;
+  if (k.hb) sb -= A[5] * 0.5f * k.rfb * wbn * rdz * k.rhomi;
   o.sb = sb;
   return o;
 }
@@ -237,10 +237,13 @@ __device__ __forceinline__ AcCol acoustic_col(const Cols& c, int k, int nz) {
   q.ht = k + 1 < nz;
   q.pi0 = c.pi0[k];
   q.rho = c.rho[k];
+  q.rhoi = c.rho_inv[k];
   q.pi0m = q.hb ? c.pi0[k - 1] : 0.f;
   q.rhom = q.hb ? c.rho[k - 1] : 1.f;
+  q.rhomi = q.hb ? c.rho_inv[k - 1] : 1.f;
   q.pi0p = q.ht ? c.pi0[k + 1] : 0.f;
   q.rhop = q.ht ? c.rho[k + 1] : 1.f;
+  q.rhopi = q.ht ? c.rho_inv[k + 1] : 1.f;
   q.rfb = c.rho_face[k];
   q.rft = c.rho_face[k + 1];
   q.dzb = c.dpi0dz[k];
@@ -437,19 +440,19 @@ __global__ void __launch_bounds__(AB) k_stage_pointwise_vjp(Dims d, Phys ph, Col
     float cw = 0.f, wb = 0.f;
     const float Rw = LD(a.Rwb, id);
     if (k >= 1 && k < nz) {
-      const float den = 0.5f * (c.rho[k - 1] + c.rho[k]);
-      cw = Rw / den;
-      wb = Rw * 0.5f * (LD(a.div, id - plane) + LD(a.div, id)) / den;
+      const float deni = c.rho_w_inv[k];   // 1 / (0.5 (rho0(k-1) + rho0(k)))
+      cw = Rw * deni;
+      wb = Rw * 0.5f * (LD(a.div, id - plane) + LD(a.div, id)) * deni;
     }
     a.cb[2][id] = cw;
     a.xsb.w[id] += wb;
     if (a.sgsb_w && k >= 1 && k < nz) a.sgsb_w[id] += Rw;
   }
   if (k >= nz) return;
-  const float r = c.rho[k];
+  const float ri = c.rho_inv[k];   // products with the correctly rounded 1 / rho0 instead of divisions
   // ---- scalars
   const float Tb = LD(a.Tnb, id), Qb = LD(a.qnb, id);
-  const float cT = a.dts * Tb / r, cQ = a.dts * Qb / r;
+  const float cT = a.dts * Tb * ri, cQ = a.dts * Qb * ri;
   a.cb[3][id] = cT;
   a.cb[4][id] = cQ;
   const float dv = LD(a.div, id);
@@ -464,19 +467,19 @@ __global__ void __launch_bounds__(AB) k_stage_pointwise_vjp(Dims d, Phys ph, Col
   }
   // ---- u, v points
   const float Ru = LD(a.Rub, id), Rv = LD(a.Rvb, id);
-  a.cb[0][id] = Ru / r;
-  a.cb[1][id] = Rv / r;
-  float ub = Ru * 0.5f * (LD(a.div, row + j * nx + im) + dv) / r;
-  float vb = Rv * 0.5f * (LD(a.div, row + jm * nx + i) + dv) / r;
+  a.cb[0][id] = Ru * ri;
+  a.cb[1][id] = Rv * ri;
+  float ub = Ru * 0.5f * (LD(a.div, row + j * nx + im) + dv) * ri;
+  float vb = Rv * 0.5f * (LD(a.div, row + jm * nx + i) + dv) * ri;
   if (a.sgsb_u) {
     a.sgsb_u[id] += Ru;
     a.sgsb_v[id] += Rv;
   }
   // divergence adjoint of this cell from the phi*div terms of its u, v, w points
-  dvb += 0.5f / r * (Ru * LD(a.xs.u, id) + LD(a.Rub, row + j * nx + ip) * LD(a.xs.u, row + j * nx + ip));
-  dvb += 0.5f / r * (Rv * LD(a.xs.v, id) + LD(a.Rvb, row + jp * nx + i) * LD(a.xs.v, row + jp * nx + i));
-  if (k >= 1) dvb += 0.5f * LD(a.Rwb, id) * LD(a.xs.w, id) / (0.5f * (c.rho[k - 1] + r));
-  if (k + 1 < nz) dvb += 0.5f * LD(a.Rwb, id + plane) * LD(a.xs.w, id + plane) / (0.5f * (r + c.rho[k + 1]));
+  dvb += 0.5f * ri * (Ru * LD(a.xs.u, id) + LD(a.Rub, row + j * nx + ip) * LD(a.xs.u, row + j * nx + ip));
+  dvb += 0.5f * ri * (Rv * LD(a.xs.v, id) + LD(a.Rvb, row + jp * nx + i) * LD(a.xs.v, row + jp * nx + i));
+  if (k >= 1) dvb += 0.5f * LD(a.Rwb, id) * LD(a.xs.w, id) * c.rho_w_inv[k];
+  if (k + 1 < nz) dvb += 0.5f * LD(a.Rwb, id + plane) * LD(a.xs.w, id + plane) * c.rho_w_inv[k + 1];
   // Coriolis: R_u += f v4, R_v -= f u4 (both cor_opt 1 and 2 are linear in the winds)
   if (ph.cor_opt) {
     const float f4 = 0.25f * ph.f_cor;
@@ -692,7 +695,7 @@ __global__ void __launch_bounds__(AB) k_smag_lin(Dims d, Phys ph, Cols c, State 
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / d.plane());
   const int id = (int)t;
-  const float r = c.rho[k];
+  const float r = c.rho[k], ri = c.rho_inv[k];
   const int ip = wrap(i + 1, nx), jp = wrap(j + 1, ny);
   const float s11 = r * (LD(s.u, d.at(ip, j, k)) - LD(s.u, id)) * ph.rdx;
   const float s22 = r * (LD(s.v, d.at(i, jp, k)) - LD(s.v, id)) * ph.rdy;
@@ -712,8 +715,8 @@ __global__ void __launch_bounds__(AB) k_smag_lin(Dims d, Phys ph, Cols c, State 
   }
   s13 *= r;
   s23 *= r;
-  const float s2 = (2.f * (s11 * s11 + s22 * s22 + s33 * s33) + 4.f * (s12 * s12 + s13 * s13 + s23 * s23)) / (r * r);
-  const float s2n2 = s2 - n2 / (float)kPrandtl;
+  const float s2 = (2.f * (s11 * s11 + s22 * s22 + s33 * s33) + 4.f * (s12 * s12 + s13 * s13 + s23 * s23)) * (ri * ri);
+  const float s2n2 = s2 - n2 * kInvPrandtl;
   const float km = s2n2 > 0.f ? ph.smag_l2 * sqrtf(s2n2) : 0.f;
   o.s[0][id] = s11; o.s[1][id] = s22; o.s[2][id] = s33; o.s[3][id] = s12; o.s[4][id] = s13; o.s[5][id] = s23;
   o.km[id] = km;
@@ -729,27 +732,27 @@ __global__ void __launch_bounds__(AB) k_smag_tau_vjp(Dims d, Phys ph, Cols c, St
   const int id = (int)t;
   const int im = wrapx(i - 1, nx), ip = wrapx(i + 1, nx), jm = wrapx(j - 1, ny), jp = wrapx(j + 1, ny);
   const float rdx = ph.rdx, rdy = ph.rdy, rdz = ph.rdz;
-  const float r = c.rho[k];
+  const float r = c.rho[k], ri = c.rho_inv[k];   // ri: the correctly rounded 1 / rho0, multiplied instead of divided
   auto at = [&](int ii, int jj, int kk) { return (kk * ny + jj) * nx + ii; };
   const float* U = a.gu;
   const float* V = a.gv;
   const float* W = a.gw;
   // tau11, tau22, tau33
-  a.tb[0][id] = (LD(U, at(ip, j, k)) - LD(U, id)) * rdx / r;
-  a.tb[1][id] = (LD(V, at(i, jp, k)) - LD(V, id)) * rdy / r;
+  a.tb[0][id] = (LD(U, at(ip, j, k)) - LD(U, id)) * rdx * ri;
+  a.tb[1][id] = (LD(V, at(i, jp, k)) - LD(V, id)) * rdy * ri;
   float t33 = 0.f;
-  if (k >= 1) t33 -= LD(W, id) * rdz / c.rho_wext[k];
-  if (k + 1 <= nz - 1) t33 += LD(W, id + plane) * rdz / c.rho_wext[k + 1];
+  if (k >= 1) t33 -= LD(W, id) * rdz * c.rho_wext_inv[k];
+  if (k + 1 <= nz - 1) t33 += LD(W, id + plane) * rdz * c.rho_wext_inv[k + 1];
   a.tb[2][id] = t33;
   // tau12 through d12v (sgs_u) and d12u (sgs_v)
   {
     auto d12v = [&](int cc, int jf) {  // adjoint of (t12(cc,jf) - t12(cc,jf-1)) rdy
       const int c1 = wrapx(cc + 1, nx), c0 = wrapx(cc, nx), j0 = wrapx(jf, ny), j1 = wrapx(jf - 1, ny);
-      return -0.25f / r * (LD(U, at(c1, j0, k)) + LD(U, at(c0, j1, k)) + LD(U, at(c1, j1, k)) + LD(U, at(c0, j0, k)));
+      return -0.25f * ri * (LD(U, at(c1, j0, k)) + LD(U, at(c0, j1, k)) + LD(U, at(c1, j1, k)) + LD(U, at(c0, j0, k)));
     };
     auto d12u = [&](int q, int rr) {  // adjoint of (t12(q,rr) - t12(q-1,rr)) rdx
       const int q0 = wrapx(q, nx), q1 = wrapx(q - 1, nx), r0 = wrapx(rr, ny), r1 = wrapx(rr + 1, ny);
-      return -0.25f / r * (LD(V, at(q0, r1, k)) + LD(V, at(q1, r0, k)) + LD(V, at(q0, r0, k)) + LD(V, at(q1, r1, k)));
+      return -0.25f * ri * (LD(V, at(q0, r1, k)) + LD(V, at(q1, r0, k)) + LD(V, at(q0, r0, k)) + LD(V, at(q1, r1, k)));
     };
     a.tb[3][id] = rdy * (d12v(i, j) - d12v(i, j + 1)) + rdx * (d12u(i, j) - d12u(i + 1, j));
   }
@@ -758,12 +761,12 @@ __global__ void __launch_bounds__(AB) k_smag_tau_vjp(Dims d, Phys ph, Cols c, St
     float t13 = 0.f, t23 = 0.f;
     for (int kf = k; kf <= k + 1; ++kf) {
       if (kf < 1 || kf > nz - 1) continue;
-      const float cw = -0.5f / c.rho_wext[kf];
+      const float cw = -0.5f * c.rho_wext_inv[kf];
       t13 += cw * (LD(W, at(im, j, kf)) - LD(W, at(ip, j, kf))) / (2.f * ph.dx);
       t23 += cw * (LD(W, at(i, jm, kf)) - LD(W, at(i, jp, kf))) / (2.f * ph.dy);
       // d13s(cc, k') = (to_w0(t13(cc), k'+1) - to_w0(t13(cc), k')) rdz enters sgs_u(cc), sgs_u(cc+1)
-      auto d13s = [&](int kk) { return -0.5f / c.rho[kk] * (LD(U, at(ip, j, kk)) + LD(U, at(i, j, kk))); };
-      auto d23s = [&](int kk) { return -0.5f / c.rho[kk] * (LD(V, at(i, jp, kk)) + LD(V, at(i, j, kk))); };
+      auto d13s = [&](int kk) { return -0.5f * c.rho_inv[kk] * (LD(U, at(ip, j, kk)) + LD(U, at(i, j, kk))); };
+      auto d23s = [&](int kk) { return -0.5f * c.rho_inv[kk] * (LD(V, at(i, jp, kk)) + LD(V, at(i, j, kk))); };
       t13 += 0.5f * rdz * (d13s(kf - 1) - d13s(kf));
       t23 += 0.5f * rdz * (d23s(kf - 1) - d23s(kf));
     }
@@ -772,8 +775,8 @@ __global__ void __launch_bounds__(AB) k_smag_tau_vjp(Dims d, Phys ph, Cols c, St
   }
   // scalar diffusion of theta and qv: direct terms and K_h
   {
-    const float khc = LD(l.km, id) / (float)kPrandtl;
-    auto kh = [&](int q) { return LD(l.km, q) / (float)kPrandtl; };
+    const float khc = LD(l.km, id) * kInvPrandtl;
+    auto kh = [&](int q) { return LD(l.km, q) * kInvPrandtl; };
     const int nb[4] = {at(im, j, k), at(ip, j, k), at(i, jm, k), at(i, jp, k)};
     float khb = 0.f;
     for (int fld = 0; fld < 2; ++fld) {
@@ -783,23 +786,23 @@ __global__ void __launch_bounds__(AB) k_smag_tau_vjp(Dims d, Phys ph, Cols c, St
       float ab = 0.f;
       // x faces i (west) and i+1 (east), y faces j and j+1
       {
-        const float fw = (g0 - LD(G, nb[0])) * rdx / r, fe = (LD(G, nb[1]) - g0) * rdx / r;
+        const float fw = (g0 - LD(G, nb[0])) * rdx * ri, fe = (LD(G, nb[1]) - g0) * rdx * ri;
         const float k8w = 0.5f * (khc + kh(nb[0])), k8e = 0.5f * (kh(nb[1]) + khc);
         ab += -r * rdx * (fw * k8w - fe * k8e);
         khb += 0.5f * (fw * (-r * (a0 - LD(A, nb[0])) * rdx) + fe * (-r * (LD(A, nb[1]) - a0) * rdx));
-        const float fs = (g0 - LD(G, nb[2])) * rdy / r, fn = (LD(G, nb[3]) - g0) * rdy / r;
+        const float fs = (g0 - LD(G, nb[2])) * rdy * ri, fn = (LD(G, nb[3]) - g0) * rdy * ri;
         const float k8s = 0.5f * (khc + kh(nb[2])), k8n = 0.5f * (kh(nb[3]) + khc);
         ab += -r * rdy * (fs * k8s - fn * k8n);
         khb += 0.5f * (fs * (-r * (a0 - LD(A, nb[2])) * rdy) + fn * (-r * (LD(A, nb[3]) - a0) * rdy));
       }
       if (k >= 1) {  // bottom face k
-        const float fb = g0 * rdz / r - LD(G, id - plane) * rdz / c.rho[k - 1];
+        const float fb = g0 * rdz * ri - LD(G, id - plane) * rdz * c.rho_inv[k - 1];
         const float k8 = 0.5f * (kh(id - plane) + khc);
         ab += -c.rho_wext[k] * k8 * rdz * fb;
         khb += 0.5f * fb * (-c.rho_wext[k] * (a0 - LD(A, id - plane)) * rdz);
       }
       if (k + 1 <= nz - 1) {  // top face k+1
-        const float ft = LD(G, id + plane) * rdz / c.rho[k + 1] - g0 * rdz / r;
+        const float ft = LD(G, id + plane) * rdz * c.rho_inv[k + 1] - g0 * rdz * ri;
         const float k8 = 0.5f * (khc + kh(id + plane));
         ab += c.rho_wext[k + 1] * k8 * rdz * ft;
         khb += 0.5f * ft * (-c.rho_wext[k + 1] * (LD(A, id + plane) - a0) * rdz);
@@ -815,9 +818,9 @@ __global__ void __launch_bounds__(AB) k_smag_s_vjp(Dims d, Cols c, SmagLin l, Sm
   const long long t = (long long)blockIdx.x * AB + threadIdx.x;
   if (t >= d.cells()) return;
   const int id = (int)t, k = (int)(t / d.plane());
-  const float r = c.rho[k], km = LD(l.km, id);
+  const float ri = c.rho_inv[k], km = LD(l.km, id);
   float s[6], tb[6];
-  float kmb = LD(a.khb, id) / (float)kPrandtl;
+  float kmb = LD(a.khb, id) * kInvPrandtl;
   for (int q = 0; q < 6; ++q) {
     s[q] = LD(l.s[q], id);
     tb[q] = LD(a.tb[q], id);
@@ -825,8 +828,8 @@ __global__ void __launch_bounds__(AB) k_smag_s_vjp(Dims d, Cols c, SmagLin l, Sm
   }
   if (a.kmkb) a.kmkb[id] = kmb * km;
   const float S2b = kmb * LD(l.kS, id);
-  for (int q = 0; q < 6; ++q) a.sb[q][id] = -2.f * km * tb[q] + S2b * (q < 3 ? 4.f : 8.f) * s[q] / (r * r);
-  a.n2b[id] = -S2b / (float)kPrandtl;
+  for (int q = 0; q < 6; ++q) a.sb[q][id] = -2.f * km * tb[q] + S2b * (q < 3 ? 4.f : 8.f) * s[q] * (ri * ri);
+  a.n2b[id] = -S2b * kInvPrandtl;
 }
 
 // adjoint of compute_deformation and compute_nm: winds and theta / qv

@@ -103,6 +103,7 @@ __global__ void k_build_columns(int nz, double dz, double theta_ref, const doubl
   float* dpi0dz = tab + 9 * S;
   float* rho_inv = tab + 10 * S;
   float* rho_w_inv = tab + 11 * S;
+  float* rho_wext_inv = tab + 12 * S;
   for (int f = threadIdx.x; f <= nz; f += blockDim.x) {
     if (f < nz) {
       const int L = f + 1;
@@ -125,6 +126,7 @@ __global__ void k_build_columns(int nz, double dz, double theta_ref, const doubl
     else
       we = rf;
     rho_wext[f] = (float)we;
+    rho_wext_inv[f] = (float)(1.0 / (double)(float)we);
     dpi0dz[f] = (float)((pi0[f + 1] - pi0[f]) / dz);
     // the face density of w's advective tendency, formed in FP32 as the kernels form it
     rho_w_inv[f] = (f == 0 || f == nz) ? 0.f : (float)(1.0 / (double)(0.5f * ((float)rho0[f] + (float)rho0[f + 1])));

@@ -54,7 +54,8 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_smag_a(Dims d, Phys ph, Cols c, 
   }
   s13 = r * s13;
   s23 = r * s23;
-  const float s2 = (2.f * (s11 * s11 + s22 * s22 + s33 * s33) + 4.f * (s12 * s12 + s13 * s13 + s23 * s23)) / (r * r);
+  const float ri = c.rho_inv[k];   // products with the correctly rounded reciprocal instead of divisions
+  const float s2 = (2.f * (s11 * s11 + s22 * s22 + s33 * s33) + 4.f * (s12 * s12 + s13 * s13 + s23 * s23)) * (ri * ri);
   float n2;
   if (k == 0)
     n2 = ext3(n2_face(d, ph, s, i, j, 1), n2_face(d, ph, s, i, j, 2), n2_face(d, ph, s, i, j, 3));
@@ -62,7 +63,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_smag_a(Dims d, Phys ph, Cols c, 
     n2 = ext3(n2_face(d, ph, s, i, j, nz - 1), n2_face(d, ph, s, i, j, nz - 2), n2_face(d, ph, s, i, j, nz - 3));
   else
     n2 = 0.5f * (n2_face(d, ph, s, i, j, k) + n2_face(d, ph, s, i, j, k + 1));
-  float s2n2 = s2 - n2 / (float)kPrandtl;
+  float s2n2 = s2 - n2 * kInvPrandtl;
   s2n2 = s2n2 > 0.f ? s2n2 : 0.f;
   const float km = ph.smag_l2 * sqrtf(s2n2);
   o.t11[id] = -2.f * km * s11;
@@ -71,7 +72,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_smag_a(Dims d, Phys ph, Cols c, 
   o.t12[id] = -2.f * km * s12;
   o.t13[id] = -2.f * km * s13;
   o.t23[id] = -2.f * km * s23;
-  o.kh[id] = km / (float)kPrandtl;
+  o.kh[id] = km * kInvPrandtl;
   if (o.n2) o.n2[id] = n2;
   if (o.km) o.km[id] = km;
 }
@@ -94,15 +95,15 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_smag_b(Dims d, Phys ph, Cols c, 
     float sw = 0.f;
     if (k > 0 && k < nz) {
       const float d33 = (T(t.t33, i, j, k) - T(t.t33, i, j, k - 1)) * rdz;
-      auto g13 = [&](int kk) { return (T(t.t13, ip, j, kk) - T(t.t13, im, j, kk)) / (2.f * ph.dx); };
-      auto g23 = [&](int kk) { return (T(t.t23, i, jp, kk) - T(t.t23, i, jm, kk)) / (2.f * ph.dy); };
-      sw = -(to_w0(g13, k, nz) + to_w0(g23, k, nz) + d33) / c.rho_wext[k];
+      auto g13 = [&](int kk) { return (T(t.t13, ip, j, kk) - T(t.t13, im, j, kk)) * (0.5f * rdx); };
+      auto g23 = [&](int kk) { return (T(t.t23, i, jp, kk) - T(t.t23, i, jm, kk)) * (0.5f * rdy); };
+      sw = -(to_w0(g13, k, nz) + to_w0(g23, k, nz) + d33) * c.rho_wext_inv[k];
     }
     o.w[d.at(i, j, k)] = sw;
   }
   if (k >= nz) return;
   const int id = d.at(i, j, k);
-  const float r = c.rho[k];
+  const float r = c.rho[k], ri = c.rho_inv[k];
   // ---------------------------------------------------------------- u point (west face of cell i)
   {
     const float d11 = (T(t.t11, i, j, k) - T(t.t11, im, j, k)) * rdx;
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_smag_b(Dims d, Phys ph, Cols c, 
       return (to_w0(g, k + 1, nz) - to_w0(g, k, nz)) * rdz;
     };
     const float d13 = 0.5f * (d13s(im) + d13s(i));
-    o.u[id] = -(d11 + d12 + d13) / r;
+    o.u[id] = -(d11 + d12 + d13) * ri;
   }
   // ---------------------------------------------------------------- v point (south face of cell j)
   {
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_smag_b(Dims d, Phys ph, Cols c, 
       return (to_w0(g, k + 1, nz) - to_w0(g, k, nz)) * rdz;
     };
     const float d23 = 0.5f * (d23s(jm) + d23s(j));
-    o.v[id] = -(d12 + d22 + d23) / r;
+    o.v[id] = -(d12 + d22 + d23) * ri;
   }
   // ---------------------------------------------------------------- scalars (cell)
   {
@@ -149,7 +150,7 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_smag_b(Dims d, Phys ph, Cols c, 
         if (f <= 0 || f >= nz) return 0.f;
         return -c.rho_wext[f] * kh8w(f) * ((T(a, i, j, f) - T(a, i, j, f - 1)) * rdz);
       };
-      return -((fx(i + 1) - fx(i)) * rdx + (fy(j + 1) - fy(j)) * rdy + (fz(k + 1) - fz(k)) * rdz) / r;
+      return -((fx(i + 1) - fx(i)) * rdx + (fy(j + 1) - fy(j)) * rdy + (fz(k + 1) - fz(k)) * rdz) * ri;
     };
     o.T[id] = diffuse(s.T);
     o.q[id] = diffuse(s.q);

@@ -38,6 +38,7 @@ constexpr float kWepsTheta = 1.0e-17f;  // one_step_integration.py:905
 constexpr float kWepsQv = 1.0e-18f;     // one_step_integration.py:913
 constexpr float kDivDamp = 1.1f;        // one_step_integration.py:546
 constexpr double kPrandtl = 1.0 / 3.0;  // turbulence.py:432
+constexpr float kInvPrandtl = 3.0f;     // 1 / kPrandtl, exact (x / Pr is x * 3)
 constexpr double kCs = 0.18;            // turbulence.py:433
 // fmin(1e30, .) of the reference (advection.py:322) would square to inf in FP32; the cap
 // below keeps every weight finite.  It only differs from the reference where a ratio
@@ -66,6 +67,7 @@ struct Cols {
   const float* dpi0dz;    // nz+1  (pi0_pad[f+1] - pi0_pad[f]) / dz
   const float* rho_inv;   // nz    1 / rho (of the FP32 rho), correctly rounded
   const float* rho_w_inv; // nz+1  1 / (0.5f * (rho[f-1] + rho[f])) on interior faces, 0 at f = 0 and nz
+  const float* rho_wext_inv; // nz+1  1 / rho_wext, correctly rounded
 };
 
 struct Phys {
@@ -372,7 +374,7 @@ cudaError_t launch_export_interior(const Dims&, const float* src, int kind, doub
 // FP64 base state
 cudaError_t launch_hydrostatic(int nz, double dz, const double* theta0, const double* qv0, double* pi0,
                                double* rho0, cudaStream_t);
-constexpr int kColumnRows = 12;   // rows of nz + 2 floats in the column table (the Cols fields, in order)
+constexpr int kColumnRows = 13;   // rows of nz + 2 floats in the column table (the Cols fields, in order)
 cudaError_t launch_build_columns(int nz, double dz, double theta_ref, const double* theta0, const double* qv0,
                                  const double* pi0, const double* rho0, float* table, cudaStream_t);
 // FP64 budgets: partial sums per block into `partial` (nblocks x 4), then a final pass into out[4]
