@@ -625,7 +625,7 @@ __global__ void __launch_bounds__(tb::NT, 2) k_acoustic_pair(Dims d, Phys ph, Co
       const float wzb = has_b ? wb * (c.dpi0dz[L] + (q0 - qB) * rdz) : 0.f;
       const float wzt = has_t ? wt * (c.dpi0dz[L + 1] + (qT - q0) * rdz) : 0.f;
       const float ap = -(0.5f * (ue * gxe + uw * gxw) + 0.5f * (vn * gyn + vs * gys) +
-                         (0.5f * wzb * c.rho_face[L] + 0.5f * wzt * c.rho_face[L + 1]) / c.rho[L]);
+                         (0.5f * wzb * c.rho_face[L] + 0.5f * wzt * c.rho_face[L + 1]) * c.rho_inv[L]);
       const float dpdt = -kRdCv * ((c.pi0[L] + q0) * div) + ap;
       o.p[id] = P1c[o_e] + (kDivDamp * dpdt) * dtau;  // P1 of level n-2 shares level n's slot
       o.u[id] = uw;

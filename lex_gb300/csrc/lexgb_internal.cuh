@@ -86,9 +86,10 @@ __device__ __forceinline__ int clampi(int i, int lo, int hi) { return i < lo ? l
 // reconstruction (advection.py:305-416 and the lateral blocks :424-503)
 // ---------------------------------------------------------------------------------------------
 // WENO5 value at the face right of c; a..e ordered upwind -> downwind.
-// Approximate reciprocal and quotient (PTX rcp.approx / div.approx, flush-to-zero forms: every
-// operand here is a normal number, b + eps >= 1e-18 and weight sums >= 0.1, where the non-ftz forms
-// give the same result but spend extra instructions on the subnormal range).
+// Approximate reciprocal and quotient (PTX rcp.approx / div.approx, flush-to-zero forms, 2 ulp).
+// Used in the WENO weights, where every denominator is a normal number (b + eps >= 1e-18, weight
+// sums >= 0.1); there the non-ftz forms give the same result but spend extra instructions on the
+// subnormal range.
 __device__ __forceinline__ float rcp_approx(float x) {
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
