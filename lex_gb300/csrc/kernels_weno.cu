@@ -842,7 +842,7 @@ __device__ __forceinline__ float2 vflux6_2m(float2 m, float2 sm3, float2 sm2, fl
 }
 
 
-__global__ void __launch_bounds__(ZNT, 2) k_weno_momentum_zm(Dims d, Phys ph, Cols c, State s, MomentumArgs a,
+__global__ void __launch_bounds__(ZNT, 3) k_weno_momentum_zm(Dims d, Phys ph, Cols c, State s, MomentumArgs a,
                                                               int zc) {
   __shared__ __align__(16) float pU[2][ZPY][ZPX];
   __shared__ __align__(16) float pV[2][ZPY][ZPX];
