@@ -62,6 +62,10 @@ struct lexgb_ctx {
   double theta_ref = 0.0;
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  // host <-> device copies of the state: a copy stream beside the compute stream, one event per
+  // field, so that a field's copy overlaps the previous field's layout conversion
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t field_ev[NFIELD] = {};
   size_t fstride = 0;  // floats per field allocation (nx*ny*(nz+1))
   // FP64 padded base columns theta0 | qv0 | pi0 | rho0 and the FP32 table
   double* base64 = nullptr;
@@ -463,6 +467,8 @@ int lexgb_create(const lexgb_config* cfg, lexgb_ctx** out) {
     return fail(code, m);
   };
   cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+  for (int f = 0; f < NFIELD && e == cudaSuccess; ++f) e = cudaEventCreateWithFlags(&c->field_ev[f], cudaEventDisableTiming);
   if (e != cudaSuccess) return bail(LEXGB_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
   e = init_weno_attributes();
   if (e == cudaSuccess) e = init_acoustic_attributes();
@@ -567,6 +573,9 @@ int lexgb_destroy(lexgb_ctx* c) {
   cudaFree(c->count);
   cudaFree(c->cs_bar);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  for (int f = 0; f < NFIELD; ++f)
+    if (c->field_ev[f]) cudaEventDestroy(c->field_ev[f]);
   delete c;
   return LEXGB_OK;
 }
@@ -621,11 +630,20 @@ int lexgb_upload_state(lexgb_ctx* c, const void* const fields[6], int dtype) {
     off[f + 1] = off[f] + (padded_count(c->d, kind_of(f)) * esz + 255) / 256 * 256;
   }
   CKS(ensure_stage(c, off[NFIELD]));
+  // the copies run on the copy stream after the compute stream's earlier work (which may still
+  // read the staging buffer); each field's conversion waits for its copy
+  CK(cudaEventRecord(c->field_ev[0], c->stream));
+  CK(cudaStreamWaitEvent(c->copy_stream, c->field_ev[0], 0));
   for (int f = 0; f < NFIELD; ++f) {
     char* dst = (char*)c->stage + off[f];
-    CK(cudaMemcpyAsync(dst, fields[f], padded_count(c->d, kind_of(f)) * esz, cudaMemcpyHostToDevice, c->stream));
-    CK(launch_import_padded(c->d, dst, dtype == LEXGB_F64, kind_of(f), f == 0 ? c->theta_ref : 0.0,
-                            field_of(c->A, f), c->stream));
+    CK(cudaMemcpyAsync(dst, fields[f], padded_count(c->d, kind_of(f)) * esz, cudaMemcpyHostToDevice,
+                       c->copy_stream));
+    CK(cudaEventRecord(c->field_ev[f], c->copy_stream));
+  }
+  for (int f = 0; f < NFIELD; ++f) {
+    CK(cudaStreamWaitEvent(c->stream, c->field_ev[f], 0));
+    CK(launch_import_padded(c->d, (char*)c->stage + off[f], dtype == LEXGB_F64, kind_of(f),
+                            f == 0 ? c->theta_ref : 0.0, field_of(c->A, f), c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));
   c->state_set = true;
@@ -642,13 +660,19 @@ int lexgb_download_state(lexgb_ctx* c, void* const fields[6], int dtype) {
   size_t off[NFIELD + 1] = {0};
   for (int f = 0; f < NFIELD; ++f) off[f + 1] = off[f] + (padded_count(c->d, kind_of(f)) * esz + 255) / 256 * 256;
   CKS(ensure_stage(c, off[NFIELD]));
+  // each field's conversion on the compute stream, its copy on the copy stream after it, so that
+  // a copy overlaps the next field's conversion
   for (int f = 0; f < NFIELD; ++f) {
     if (!fields[f]) continue;
     char* src = (char*)c->stage + off[f];
     CK(launch_export_padded(c->d, field_of(c->A, f), kind_of(f), f == 0 ? c->theta_ref : 0.0, src,
                             dtype == LEXGB_F64, c->stream));
-    CK(cudaMemcpyAsync(fields[f], src, padded_count(c->d, kind_of(f)) * esz, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaEventRecord(c->field_ev[f], c->stream));
+    CK(cudaStreamWaitEvent(c->copy_stream, c->field_ev[f], 0));
+    CK(cudaMemcpyAsync(fields[f], src, padded_count(c->d, kind_of(f)) * esz, cudaMemcpyDeviceToHost,
+                       c->copy_stream));
   }
+  CK(cudaStreamSynchronize(c->copy_stream));
   CK(cudaStreamSynchronize(c->stream));
   return take_status(c);
 }

@@ -16,38 +16,51 @@ __host__ __device__ inline void padded_extents(const Dims& d, int kind, int& PX,
 
 __host__ __device__ inline int levels(const Dims& d, int kind) { return kind == 3 ? d.nz + 1 : d.nz; }
 
-// device layout <- reference padded layout (interior part; u/v drop the duplicated face)
+// Device layout <- reference padded layout (interior part; u/v drop the duplicated face), and
+// reference padded layout <- device layout with the ghosts filled as padding3_array /
+// padding3u_array / padding3v_array (one_step_integration.py:950-985).  Tiled transposes: at one y
+// row, a 32 x 32 tile of (x, level) goes through shared memory, so both the padded layout (level
+// fastest) and the device layout (x fastest) are read and written in whole rows.  Block (32, 8),
+// grid (x tiles, level tiles, rows).
+constexpr int TT = 32, TR = 8;
+
 template <typename Src>
-__global__ void k_import(Dims d, const Src* __restrict__ src, int kind, double offset, float* __restrict__ dst) {
-  const long long n = (long long)d.plane() * levels(d, kind);
+__global__ void __launch_bounds__(TT* TR) k_import_t(Dims d, const Src* __restrict__ src, int kind, double offset,
+                                                    float* __restrict__ dst) {
+  __shared__ float tile[TT][TT + 1];
   int PX, PY, PZ;
   padded_extents(d, kind, PX, PY, PZ);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % d.nx);
-    const int j = (int)((t / d.nx) % d.ny);
-    const int k = (int)(t / ((long long)d.nx * d.ny));
-    const long long s = ((long long)(i + NGX) * PY + (j + NGY)) * PZ + (k + NGZ);
-    dst[t] = (float)((double)src[s] - offset);
+  const int nl = levels(d, kind), j = blockIdx.z;
+  const int i0 = blockIdx.x * TT, k0 = blockIdx.y * TT, tx = threadIdx.x, ty = threadIdx.y;
+  for (int r = ty; r < TT; r += TR) {   // rows x = i0 + r, levels k0 + tx along the row
+    const int i = i0 + r, k = k0 + tx;
+    if (i < d.nx && k < nl)
+      tile[r][tx] = (float)((double)src[((long long)(i + NGX) * PY + (j + NGY)) * PZ + (k + NGZ)] - offset);
+  }
+  __syncthreads();
+  for (int r = ty; r < TT; r += TR) {   // rows k = k0 + r, x = i0 + tx along the row
+    const int i = i0 + tx, k = k0 + r;
+    if (i < d.nx && k < nl) dst[(long long)k * d.plane() + (long long)j * d.nx + i] = tile[tx][r];
   }
 }
 
-// reference padded layout <- device layout, ghosts filled as padding3_array / padding3u_array /
-// padding3v_array (one_step_integration.py:950-985)
 template <typename Dst>
-__global__ void k_export_padded(Dims d, const float* __restrict__ src, int kind, double offset,
-                                Dst* __restrict__ dst) {
+__global__ void __launch_bounds__(TT* TR) k_export_t(Dims d, const float* __restrict__ src, int kind, double offset,
+                                                    Dst* __restrict__ dst) {
+  __shared__ float tile[TT][TT + 1];
   int PX, PY, PZ;
   padded_extents(d, kind, PX, PY, PZ);
-  const long long n = (long long)PX * PY * PZ;
-  const int nl = levels(d, kind);
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int L = (int)(t % PZ);
-    const int q = (int)((t / PZ) % PY);
-    const int p = (int)(t / ((long long)PZ * PY));
-    const int i = wrap(p - NGX, d.nx);
-    const int j = wrap(q - NGY, d.ny);
-    const int k = clampi(L - NGZ, 0, nl - 1);
-    dst[t] = (Dst)((double)src[d.at(i, j, k)] + offset);
+  const int nl = levels(d, kind), q = blockIdx.z, j = wrap(q - NGY, d.ny);
+  const int p0 = blockIdx.x * TT, L0 = blockIdx.y * TT, tx = threadIdx.x, ty = threadIdx.y;
+  for (int r = ty; r < TT; r += TR) {   // padded levels L0 + r, padded x p0 + tx along the row
+    const int p = p0 + tx, L = L0 + r;
+    if (p < PX && L < PZ)
+      tile[r][tx] = src[(long long)clampi(L - NGZ, 0, nl - 1) * d.plane() + (long long)j * d.nx + wrap(p - NGX, d.nx)];
+  }
+  __syncthreads();
+  for (int r = ty; r < TT; r += TR) {   // padded x p0 + r, levels L0 + tx along the row
+    const int p = p0 + r, L = L0 + tx;
+    if (p < PX && L < PZ) dst[((long long)p * PY + q) * PZ + L] = (Dst)((double)tile[tx][r] + offset);
   }
 }
 
@@ -231,11 +244,11 @@ inline int blocks_for(long long n, int threads) {
 
 cudaError_t launch_import_padded(const Dims& d, const void* src, int src_f64, int kind, double offset, float* dst,
                                  cudaStream_t st) {
-  const long long n = (long long)d.plane() * levels(d, kind);
+  const dim3 g((d.nx + TT - 1) / TT, (levels(d, kind) + TT - 1) / TT, d.ny), b(TT, TR);
   if (src_f64)
-    k_import<double><<<blocks_for(n, 256), 256, 0, st>>>(d, (const double*)src, kind, offset, dst);
+    k_import_t<double><<<g, b, 0, st>>>(d, (const double*)src, kind, offset, dst);
   else
-    k_import<float><<<blocks_for(n, 256), 256, 0, st>>>(d, (const float*)src, kind, offset, dst);
+    k_import_t<float><<<g, b, 0, st>>>(d, (const float*)src, kind, offset, dst);
   return cudaGetLastError();
 }
 
@@ -243,11 +256,11 @@ cudaError_t launch_export_padded(const Dims& d, const float* src, int kind, doub
                                  cudaStream_t st) {
   int PX, PY, PZ;
   padded_extents(d, kind, PX, PY, PZ);
-  const int nb = blocks_for((long long)PX * PY * PZ, 256);
+  const dim3 g((PX + TT - 1) / TT, (PZ + TT - 1) / TT, PY), b(TT, TR);
   if (dst_f64)
-    k_export_padded<double><<<nb, 256, 0, st>>>(d, src, kind, offset, (double*)dst);
+    k_export_t<double><<<g, b, 0, st>>>(d, src, kind, offset, (double*)dst);
   else
-    k_export_padded<float><<<nb, 256, 0, st>>>(d, src, kind, offset, (float*)dst);
+    k_export_t<float><<<g, b, 0, st>>>(d, src, kind, offset, (float*)dst);
   return cudaGetLastError();
 }
 
