@@ -1242,9 +1242,12 @@ int adj_forward(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages) {
                           w.trho[s]));
     CK(launch_adv_momentum(d, c->ph, c->cols, xs, w.div[s], sg, w.Ru[s], w.Rv[s], w.Rw[s], 0, c->stream));
     AcousticIn in{A.u, A.v, A.w, A.p, w.Ru[s], w.Rv[s], w.Rw[s], w.trho[s], xs.p};
+    // the stage's theta_rho, R_u, R_v, R_w (adjacent workspace fields) persist in L2 through its sub-steps
+    cudaAccessPolicyWindow win{};
+    const bool win_on = l2_window_for(c, w.trho[s], 4 * c->fstride * sizeof(float), &win);
     for (int m = 1; m <= p.n[s]; ++m) {
       const AcousticOut o{w.ac[s][m][0], w.ac[s][m][1], w.ac[s][m][2], w.ac[s][m][3]};
-      CK(sub_step(c, in, o, (float)p.dtau[s], 0, nullptr));
+      CK(sub_step(c, in, o, (float)p.dtau[s], 0, win_on ? &win : nullptr));
       in.u = o.u; in.v = o.v; in.w = o.w; in.p = o.p;
     }
   }
@@ -1339,6 +1342,9 @@ int adj_reverse(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages, const fl
                        c->stream));
   }
   CK(cudaStreamSynchronize(c->stream));
+  // the accumulators' persisting lines (71 MB at 192 x 192 x 96) would crowd the L2 of the work
+  // that follows; return them to normal use (the step's own window re-persists its fields)
+  if (awin_on) cudaCtxResetPersistingL2Cache();
   return LEXGB_OK;
 }
 
