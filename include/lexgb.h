@@ -258,7 +258,10 @@ int lexgb_step_vjp_kept(lexgb_ctx *ctx, const float *const ybar[6], float *xbar[
  *   in w it is the gradient with respect to the input.
  * lexgb_cnn_gelu_bwd: g = dy * GELU'(pre) (pre NULL: g = dy), FP32 [npts][c] -> BF16 [npts][cpad].
  * lexgb_cnn_conv3d_dw: dw[27][cout][cin] += sum_p g[p][co] x[p+off][ci], db[cout] += sum_p g[p][co]
- *   (FP32, accumulated: zero them first); g has `gstride` channels per point.
+ *   (FP32, accumulated: zero them first); g has `gstride` channels per point.  dw is summed on the
+ *   tcgen05 tensor cores (BF16 products, FP32 accumulation in tensor memory, any nx, ny, nz) for cin
+ *   16 or 32, gstride 16 or 32 and 16-byte aligned x and g, unless lexgb_cnn_set_kernel chose
+ *   LEXGB_CNN_MMA, which (like other shapes) takes the FP32 CUDA-core reduction.
  * lexgb_cnn_adam: Adam step `step` (>= 1) of n FP32 parameters with moments m, v; optional BF16 copy.
  * Replace flax's Conv / optax in lex_dl_train.py (the reference trains with optax.lamb). */
 int lexgb_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const void *x, const void *w, const float *bias,
@@ -269,8 +272,9 @@ int lexgb_cnn_conv3d(int nx, int ny, int nz, int cin, int cout, const void *x, c
  * fits it and has at least 2^18 points, else the mma.sync kernel; LEXGB_CNN_MMA the mma.sync
  * kernel; LEXGB_CNN_TCGEN05 the
  * tcgen05 kernel only (a grid it does not fit is an error).  Set it before capturing a step graph.
- * lexgb_cnn_take_timeouts: the number of bounded waits of the tcgen05 kernel that gave up since
- * the last call (0 in normal operation; such a tile's outputs are not written), then reset. */
+ * lexgb_cnn_take_timeouts: the number of bounded waits of the tcgen05 kernels (convolution and
+ * weight gradient) that gave up since the last call (0 in normal operation; such a tile's outputs,
+ * or such a block's share of dw, are not written), then reset. */
 enum { LEXGB_CNN_AUTO = 0, LEXGB_CNN_MMA = 1, LEXGB_CNN_TCGEN05 = 2 };
 int lexgb_cnn_set_kernel(int which);
 int lexgb_cnn_take_timeouts(unsigned int *n);

@@ -639,10 +639,18 @@ extern "C" int lexgb_cnn_conv3d_dw(int nx, int ny, int nz, int cin, int cout, in
     return cnn_arg("lexgb_cnn_conv3d_dw: bad argument (cin, cout <= 32, cout divides 256, gstride >= cout)");
   const long long npts = (long long)nx * ny * nz;
   cudaStream_t st = (cudaStream_t)stream;
-  dim3 grid((unsigned)((npts + SLAB - 1) / SLAB), 27);
-  const size_t smem = (size_t)SLAB * (cin + cout) * sizeof(float);
-  k_conv3d_dw<<<grid, 256, smem, st>>>(nx, ny, nz, cin, cout, gstride, (const __nv_bfloat16*)x,
-                                       (const __nv_bfloat16*)g, dw);
+  if (g_conv_kernel != LEXGB_CNN_MMA && conv_dw_tc_fits(nx, ny, nz, cin, cout, gstride, x, g, dw)) {
+    const cudaError_t e = launch_conv_dw_tc(nx, ny, nz, cin, cout, gstride, x, g, dw, st);
+    if (e != cudaSuccess) return cnn_status(e, "lexgb_cnn_conv3d_dw (tcgen05)");
+  } else if (g_conv_kernel == LEXGB_CNN_TCGEN05) {
+    return cnn_arg("lexgb_cnn_conv3d_dw: the tcgen05 kernel needs cin 16 or 32, gstride 16 or 32, cout <= gstride "
+                   "and 16-byte aligned x and g");
+  } else {
+    dim3 grid((unsigned)((npts + SLAB - 1) / SLAB), 27);
+    const size_t smem = (size_t)SLAB * (cin + cout) * sizeof(float);
+    k_conv3d_dw<<<grid, 256, smem, st>>>(nx, ny, nz, cin, cout, gstride, (const __nv_bfloat16*)x,
+                                         (const __nv_bfloat16*)g, dw);
+  }
   if (db) k_bias_grad<<<256, 256, 0, st>>>(npts, cout, gstride, (const __nv_bfloat16*)g, db);
   return cnn_status(cudaGetLastError(), "lexgb_cnn_conv3d_dw");
 }

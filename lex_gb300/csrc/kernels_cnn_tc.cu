@@ -341,6 +341,218 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3d_tc(const __grid_constant_
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Weight gradient on the tensor cores:
+//
+//   dW[tap][co][ci] += sum over points p of g[p][co] x[p + off(tap)][ci]
+//
+// as D[M][N] += A[M][K] B[K][N] with K = the 128 points of an 8 (x) x 16 (y) tile at one level,
+// N = the gradient's channels co (16 or 32) and M = 128 rows (dy shift s, input channel ci): the
+// rows of A are the input plane read 16 / CG (4 or 8) rows apart, so one MMA covers the y offsets
+// -1, 0, +1 (and spare shifts whose rows are dropped).  Each of the nine (dz, dx) offset pairs has
+// its own accumulator in tensor memory; a block keeps them over all the (tile, level chunk) items
+// it takes and adds them to dW once, at the end.  Both operands are MN-major (the channels are
+// the contiguous 16 bytes of a core matrix; its 8 rows are 8 consecutive points along x):
+//   x planes  Xsm[HY][CG][10][8]   halo rows y0-1 .. y0+14+SH, all channel groups of a row
+//                                  together (a 5-D tensor map with the channel group as its own
+//                                  dimension), so the next M block (next channel group, or the
+//                                  next row after the last group) is 160 bytes on (SBO) and the
+//                                  next K block (the next row of the tile) one halo row on (LBO)
+//   gradient  Gsm[NP/8][16][8][8]  next N block = next channel group, 2048 bytes (SBO); next K
+//                                  block = next row, 128 bytes (LBO)
+// Warp 4 loads plane p of x (with its halo; zero outside the grid) and, for the levels of the
+// item, plane p of g into one slot of a ring; warp 5 issues the 72 MMAs of a level (3 dz x 3 dx x
+// 8 pairs of rows); warps 0-3 wait for the last MMA, read their lane quarter of the nine
+// accumulators and add the rows of the y offsets -1..+1 to dW (atomicAdd).
+template <int CG, int NP>
+struct DwLayout {
+  static constexpr int SH = 16 / CG;                        // y shifts in the 128 rows of M
+  static constexpr int HY = TC_TY + SH - 1;                 // halo rows of an x plane
+  static constexpr int ROW_BYTES = CG * TC_HX * 16;         // one halo row, all channel groups
+  static constexpr int X_BYTES = HY * ROW_BYTES;
+  static constexpr int X_PAD = (X_BYTES + 127) / 128 * 128;
+  static constexpr int G_GROUP = TC_TY * TC_TX * 16;        // one 8-channel group of a gradient tile
+  static constexpr int G_BYTES = NP / 8 * G_GROUP;
+  static constexpr int SLOT = X_PAD + G_BYTES;
+  static constexpr int R = 6;                               // ring slots
+  static constexpr int TMEM_COLS = 9 * NP <= 256 ? 256 : 512;
+  static constexpr int BAR_BYTES = (2 * R + 1) * 8 + 16;
+  // + 4 KB after the barriers: an operand's core matrices, read with the two descriptor strides
+  // either way round, stay inside the allocation
+  static constexpr size_t NEED = 128 + (size_t)R * SLOT + BAR_BYTES + 4096;
+  // at most 512 / TMEM_COLS blocks per SM, so that no block waits for another's tensor memory
+  static constexpr size_t FLOOR = TMEM_COLS == 512 ? 120 * 1024 : 80 * 1024;
+  static constexpr size_t BYTES = NEED < FLOOR ? FLOOR : NEED;
+};
+
+// a 5-D box into shared memory, completing on an mbarrier
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            int c4, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+      "%5, %6}], [%7];" ::"r"(dst),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+      : "memory");
+}
+
+// Bounded wait with a back-off between polls (about a second at most), for the warps that wait out
+// the whole of a block's work; gives up early when the block's abort flag is set (if checked).
+__device__ __forceinline__ bool mbar_wait_long(uint32_t bar, uint32_t parity, const volatile int* abort) {
+  for (long long i = 0; i < (1ll << 22); ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (abort && *abort) return false;
+    __nanosleep(256);
+  }
+  return false;
+}
+
+template <int CG, int NP>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_conv3d_dw_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap gmap, int nx,
+                   int ny, int nz, int zc, int cin, int cout, float* __restrict__ dw) {
+  using L = DwLayout<CG, NP>;
+  constexpr int R = L::R;
+  extern __shared__ unsigned char tc_raw[];
+  const uint32_t raw_s = smem_u32(tc_raw);
+  unsigned char* smem = tc_raw + ((128u - (raw_s & 127u)) & 127u);
+  const uint32_t ring_s = smem_u32(smem), bar_s = ring_s + R * L::SLOT;
+  auto slot = [&](long long j) { return ring_s + (uint32_t)(j % R) * L::SLOT; };
+  auto full = [&](long long j) { return bar_s + 8u * (uint32_t)(j % R); };
+  auto empty = [&](long long j) { return bar_s + 8u * (R + (uint32_t)(j % R)); };
+  const uint32_t done = bar_s + 8u * (2 * R);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + R * L::SLOT + (2 * R + 1) * 8);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 5) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(L::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < R; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(empty(s), 1);
+    }
+    mbar_init(done, 1);
+    *abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  const int tiles_x = (nx + TC_TX - 1) / TC_TX, tiles_y = (ny + TC_TY - 1) / TC_TY;
+  const int chunks = (nz + zc - 1) / zc, items = tiles_x * tiles_y * chunks;
+
+  if (warp == 4) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      long long j = 0;
+      bool ok = true;
+      for (int it = blockIdx.x; it < items && ok; it += gridDim.x) {
+        const int x0 = (it % tiles_x) * TC_TX, y0 = ((it / tiles_x) % tiles_y) * TC_TY;
+        const int z0 = (it / (tiles_x * tiles_y)) * zc, z1 = min(z0 + zc, nz);
+        for (int p = z0 - 1; p <= z1; ++p, ++j) {
+          if (j >= R && !mbar_wait(empty(j), (uint32_t)((j / R - 1) & 1), abort)) {
+            atomicAdd(&g_tc_timeouts, 1u);
+            *abort = 1;
+            ok = false;
+            break;
+          }
+          const bool with_g = p >= z0 && p < z1;
+          mbar_expect_tx(full(j), L::X_BYTES + (with_g ? L::G_BYTES : 0));
+          tma_load_5d(slot(j), &xmap, 0, x0 - 1, 0, y0 - 1, p, full(j));
+          if (with_g)
+            for (int cg = 0; cg < NP / 8; ++cg)
+              tma_load_4d(slot(j) + L::X_PAD + cg * L::G_GROUP, &gmap, cg * 8, x0, y0, p, full(j));
+        }
+      }
+      // the copies this thread issued have landed before the block's memory goes (bounded)
+      for (long long jj = j - 1; jj >= 0 && jj >= j - R; --jj) mbar_wait_long(full(jj), (uint32_t)((jj / R) & 1), nullptr);
+    }
+  } else if (warp == 5) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc_idesc(128, NP) | (1u << 15) | (1u << 16);   // A and B MN-major
+      long long j = 0;
+      bool ok = true, first = true;
+      for (int it = blockIdx.x; it < items && ok; it += gridDim.x) {
+        const int z0 = (it / (tiles_x * tiles_y)) * zc, z1 = min(z0 + zc, nz);
+        const long long jb = j;   // load index of plane z0 - 1
+        for (int z = z0; z < z1 && ok; ++z) {
+          const long long jz = jb + (z - z0);   // plane z - 1; planes z and z + 1 follow
+          for (int q = (z == z0 ? 0 : 2); q <= 2 && ok; ++q) ok = mbar_wait(full(jz + q), (uint32_t)(((jz + q) / R) & 1), abort);
+          if (!ok) {
+            atomicAdd(&g_tc_timeouts, 1u);
+            *abort = 1;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint64_t b0 = smem_desc(slot(jz + 1) + L::X_PAD, 128, L::G_GROUP);
+#pragma unroll
+          for (int dz = 0; dz < 3; ++dz) {
+            const uint64_t a0 = smem_desc(slot(jz + dz), L::ROW_BYTES, TC_HX * 16);
+#pragma unroll
+            for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+              for (int m = 0; m < 8; ++m) {
+                const uint64_t ad = a0 + (uint64_t)((2 * m * L::ROW_BYTES + dx * 16) >> 4);
+                const uint64_t bd = b0 + (uint64_t)((2 * m * 128) >> 4);
+                mma_bf16_tc(tmem + (uint32_t)((dz * 3 + dx) * NP), ad, bd, idesc, (first && m == 0) ? 0u : 1u);
+              }
+          }
+          first = false;
+          mma_commit(empty(jz));   // plane z - 1 is not read again
+        }
+        if (!ok) break;
+        mma_commit(empty(jb + (z1 - z0)));       // planes z1 - 1 and z1
+        mma_commit(empty(jb + (z1 - z0) + 1));
+        j = jb + (z1 - z0) + 2;
+      }
+      mma_commit(done);
+      mbar_wait_long(done, 0, nullptr);   // the MMAs are complete before the tensor memory goes
+    }
+  } else {
+    // ---------------- warps 0-3: the accumulators into dW ----------------
+    const bool got = __all_sync(0xffffffffu, mbar_wait_long(done, 0, abort));
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int r = 32 * warp + lane, b = r >> 3, s = b / CG, ci = (b % CG) * 8 + (r & 7);
+    if (got && !*abort && (4 * warp) / CG <= 2) {   // the warp holds rows of the y offsets -1..+1
+      const bool mine = s <= 2 && ci < cin;
+#pragma unroll 1
+      for (int acc = 0; acc < 9; ++acc) {
+        float v[NP];
+#pragma unroll
+        for (int c = 0; c < NP; c += 16) tmem_load16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(acc * NP + c), v + c);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (mine) {
+          const int tap = (acc / 3) * 9 + s * 3 + acc % 3;
+          float* d = dw + (long long)tap * cout * cin + ci;
+#pragma unroll
+          for (int co = 0; co < NP; ++co)
+            if (co < cout) atomicAdd(d + (long long)co * cin, v[co]);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 5) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L::TMEM_COLS) : "memory");
+  }
+}
+
 constexpr int TC_MAX_DEVICES = 64;
 
 template <int CIN, int COUT>
@@ -438,6 +650,92 @@ cudaError_t launch_tc(int nx, int ny, int nz, const void* x, const __nv_bfloat16
                             pdl ? 1 : 0);
 }
 
+
+// activations [z][y][x][cin] BF16 as a 5-D tensor (8 channels, x, channel group, y, z): a box is a
+// plane tile of 10 x hy points with all cin / 8 groups of each row side by side
+bool make_dw_xmap(CUtensorMap* map, const void* x, int nx, int ny, int nz, int cin, int hy) {
+  EncodeTiledFn enc = tc_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[5] = {8, (cuuint64_t)nx, (cuuint64_t)(cin / 8), (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[4] = {(cuuint64_t)cin * 2, 16, (cuuint64_t)nx * cin * 2, (cuuint64_t)ny * nx * cin * 2};
+  const cuuint32_t box[5] = {8, TC_HX, (cuuint32_t)(cin / 8), (cuuint32_t)hy, 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(x), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// gradient [z][y][x][c] BF16 as a 4-D tensor (channel, x, y, z); box = one 8-channel group of an
+// 8 x 16 tile
+bool make_dw_gmap(CUtensorMap* map, const void* g, int nx, int ny, int nz, int c) {
+  EncodeTiledFn enc = tc_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)c, (cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[3] = {(cuuint64_t)c * 2, (cuuint64_t)nx * c * 2, (cuuint64_t)ny * nx * c * 2};
+  const cuuint32_t box[4] = {8, TC_TX, TC_TY, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(g), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int CG, int NP>
+cudaError_t dw_grid(int* cap) {
+  static int grid_cap[TC_MAX_DEVICES] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= TC_MAX_DEVICES) return cudaErrorInvalidDevice;
+  if (!grid_cap[dev]) {
+    using L = DwLayout<CG, NP>;
+    e = cudaFuncSetAttribute(k_conv3d_dw_tc<CG, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_conv3d_dw_tc<CG, NP>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    int sms = 0, per = 0;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv3d_dw_tc<CG, NP>, TC_THREADS, L::BYTES)) !=
+        cudaSuccess)
+      return e;
+    per = per < 1 ? 1 : per;
+    if (per > 512 / L::TMEM_COLS) per = 512 / L::TMEM_COLS;
+    grid_cap[dev] = sms * per;
+  }
+  *cap = grid_cap[dev];
+  return cudaSuccess;
+}
+
+template <int CG, int NP>
+cudaError_t launch_dw(int nx, int ny, int nz, int cin, int cout, const void* x, const void* g, float* dw,
+                      cudaStream_t st) {
+  using L = DwLayout<CG, NP>;
+  int cap = 0;
+  cudaError_t e = dw_grid<CG, NP>(&cap);
+  if (e != cudaSuccess) return e;
+  CUtensorMap xmap, gmap;
+  if (!make_dw_xmap(&xmap, x, nx, ny, nz, cin, L::HY) || !make_dw_gmap(&gmap, g, nx, ny, nz, NP))
+    return cudaErrorInvalidValue;
+  // level chunks: the count that ends soonest when every block takes ceil(items / blocks) items
+  // of chunk + 1 plane times (ties: fewer items, each of which loads two extra planes)
+  const long long tiles = (long long)((nx + TC_TX - 1) / TC_TX) * ((ny + TC_TY - 1) / TC_TY);
+  int zc = nz;
+  long long best = -1;
+  for (int nch = 1; nch <= nz; ++nch) {
+    const int z = (nz + nch - 1) / nch;
+    const long long items = tiles * ((nz + z - 1) / z), blocks = items < cap ? items : cap;
+    const long long cost = (items + blocks - 1) / blocks * (z + 1);
+    if (best < 0 || cost < best) {
+      best = cost;
+      zc = z;
+    }
+  }
+  const long long items = tiles * ((nz + zc - 1) / zc);
+  if (items > 0x7fffffffll) return cudaErrorInvalidValue;
+  const unsigned blocks = (unsigned)(items < cap ? items : cap);
+  k_conv3d_dw_tc<CG, NP><<<blocks, TC_THREADS, L::BYTES, st>>>(xmap, gmap, nx, ny, nz, zc, cin, cout, dw);
+  return cudaGetLastError();
+}
 }  // namespace
 
 bool conv_tc_fits(int nx, int ny, int nz, int cin, int cout, const void* x, const void* pre, const void* ybf,
@@ -466,7 +764,27 @@ cudaError_t conv_tc_prepare() {
   if ((e = tc_grid<16, 32>(&cap)) != cudaSuccess) return e;
   if ((e = tc_grid<32, 8>(&cap)) != cudaSuccess) return e;
   if ((e = tc_grid<32, 16>(&cap)) != cudaSuccess) return e;
-  return tc_grid<32, 32>(&cap);
+  if ((e = tc_grid<32, 32>(&cap)) != cudaSuccess) return e;
+  if ((e = dw_grid<2, 16>(&cap)) != cudaSuccess) return e;
+  if ((e = dw_grid<2, 32>(&cap)) != cudaSuccess) return e;
+  if ((e = dw_grid<4, 16>(&cap)) != cudaSuccess) return e;
+  return dw_grid<4, 32>(&cap);
+}
+
+bool conv_dw_tc_fits(int nx, int ny, int nz, int cin, int cout, int gstride, const void* x, const void* g,
+                     const float* dw) {
+  const uintptr_t align = (uintptr_t)x | (uintptr_t)g;   // 16-byte TMA bases
+  return (cin == 16 || cin == 32) && (gstride == 16 || gstride == 32) && cout > 0 && cout <= gstride && nx > 0 &&
+         ny > 0 && nz > 0 && (align & 15) == 0 && dw && tc_encoder() != nullptr;
+}
+
+cudaError_t launch_conv_dw_tc(int nx, int ny, int nz, int cin, int cout, int gstride, const void* x, const void* g,
+                              float* dw, cudaStream_t st) {
+  if (!conv_dw_tc_fits(nx, ny, nz, cin, cout, gstride, x, g, dw)) return cudaErrorInvalidValue;
+  if (cin == 16) return gstride == 16 ? launch_dw<2, 16>(nx, ny, nz, cin, cout, x, g, dw, st)
+                                      : launch_dw<2, 32>(nx, ny, nz, cin, cout, x, g, dw, st);
+  return gstride == 16 ? launch_dw<4, 16>(nx, ny, nz, cin, cout, x, g, dw, st)
+                       : launch_dw<4, 32>(nx, ny, nz, cin, cout, x, g, dw, st);
 }
 
 cudaError_t conv_tc_take_timeouts(unsigned int* n) {

@@ -133,3 +133,43 @@ def _conv_call(nx, ny, nz, cin, cout, x, w, b, pre, yb):
     return lib.lexgb_cnn_conv3d(nx, ny, nz, cin, cout, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(w.data_ptr()),
                                 ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(pre.data_ptr()),
                                 ctypes.c_void_p(yb.data_ptr()), None, 1, 5, None)
+
+
+DW_CASES = [(16, 32, 32, (32, 32, 8)), (32, 32, 32, (32, 32, 8)), (32, 8, 16, (32, 32, 8)), (16, 8, 16, (16, 16, 6)),
+            (32, 32, 32, (20, 13, 5)), (16, 32, 32, (9, 17, 3))]
+
+
+@pytest.mark.parametrize("cin,cout,gstride,dims", DW_CASES,
+                         ids=["%d-%d-%d-%dx%dx%d" % ((a, b, c) + d) for a, b, c, d in DW_CASES])
+def test_tcgen05_weight_gradient_matches_cuda_cores(conv_kernel, cin, cout, gstride, dims):
+    """lexgb_cnn_conv3d_dw on the tensor cores (tcgen05, the AUTO choice) against the FP32 CUDA-core
+    reduction (the LEXGB_CNN_MMA choice) on the same BF16 activations and gradients, including grids
+    that the 8 x 16 tiles do not divide: both sum the same exact BF16 products in FP32, in a
+    different order, so they agree to FP32 summation rounding; the bias gradient is the same kernel
+    on both."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from lex_gb300 import _lib
+    lib = _lib.load()
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    gen = torch.Generator(device="cpu").manual_seed(cin * 7 + cout + gstride + nx)
+    x = torch.randn(n, cin, generator=gen).to(torch.bfloat16).cuda()
+    g = torch.randn(n, gstride, generator=gen).to(torch.bfloat16).cuda()
+    outs = {}
+    for kernel in ("mma", "tcgen05"):
+        conv_kernel(kernel)
+        dw = torch.zeros(27, cout, cin, device="cuda")
+        db = torch.zeros(cout, device="cuda")
+        rc = lib.lexgb_cnn_conv3d_dw(nx, ny, nz, cin, cout, gstride, ctypes.c_void_p(x.data_ptr()),
+                                     ctypes.c_void_p(g.data_ptr()), ctypes.c_void_p(dw.data_ptr()),
+                                     ctypes.c_void_p(db.data_ptr()), None)
+        assert rc == 0
+        torch.cuda.synchronize()
+        outs[kernel] = (dw, db)
+    a, r = outs["tcgen05"][0], outs["mma"][0]
+    assert _rel(a, r) < 1e-5, _rel(a, r)
+    # every offset on its own (the edge offsets see fewer points)
+    for tap in range(27):
+        assert _rel(a[tap], r[tap]) < 1e-5, (tap, _rel(a[tap], r[tap]))
+    assert _rel(outs["tcgen05"][1], outs["mma"][1]) < 1e-6
