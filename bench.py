@@ -363,7 +363,7 @@ def run_lexgb(args):
     # ---- learned SGS correction fused into the coarse step (600 m x 600 m x 300 m, 32^3, dt = 3 s)
     sgs = None
     if not args.no_sgs:
-        from lex_gb300 import learned_sgs as lsgs, sgs_cnn, autograd as lag
+        from lex_gb300 import learned_sgs as lsgs, sgs_cnn, autograd as lag, _lib
         from lex_gb300.workload import warm_bubble
         net = sgs_cnn.SGSNet(seed=0, zero_last=False)
         net.w[3] *= 0.01   # corrections of the size a trained network makes
@@ -380,12 +380,46 @@ def run_lexgb(args):
             Sc.close()
             return cplain, clearn
 
+        def train_cost(dims, kernel, reps):
+            # one forward + backward of the network (input, weight and bias gradients), as a
+            # training step through the solver runs it per corrected step
+            lib = _lib.load()
+            _lib.check(lib.lexgb_cnn_set_kernel(kernel))
+            n = dims[0] * dims[1] * dims[2]
+            gen = torch.Generator(device="cpu").manual_seed(5)
+            x = torch.rand(n, 5, generator=gen).cuda().requires_grad_(True)
+            seed = torch.randn(n, 5, generator=gen).cuda()
+            params = [t.detach().clone().requires_grad_(True) for t in net.params()]
+            tnet = sgs_cnn.SGSNet(seed=0, zero_last=False)
+            tnet.w, tnet.b = params[:4], params[4:]
+            tnet.refresh()
+
+            def once():
+                out = sgs_cnn.net_apply(tnet, x, dims)
+                return torch.autograd.grad((out * seed).sum(), [x] + params)
+            once()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                once()
+            e1.record()
+            torch.cuda.synchronize()
+            _lib.check(lib.lexgb_cnn_set_kernel(0))
+            return e0.elapsed_time(e1) / reps
+
         cplain, clearn = corrected_cost((32, 32, 32), 300)
         lplain, llearn = corrected_cost((128, 128, 64), 100)
+        t_tc = train_cost((128, 128, 64), 2, 10)
+        t_legacy = train_cost((128, 128, 64), 1, 3)
         sgs = {"grid": [32, 32, 32], "dx_m": [600.0, 600.0, 300.0], "dt_s": 3.0,
                "ms_per_step_plain": cplain, "ms_per_step_learned": clearn, "cost_ratio": clearn / cplain,
                "grid_128x128x64": {"ms_per_step_plain": lplain, "ms_per_step_learned": llearn,
                                    "cost_ratio": llearn / lplain},
+               "network_fwd_bwd_128x128x64_ms": {"tcgen05": t_tc, "mma_sync_and_cuda_core_dw": t_legacy,
+                                                 "note": "net_apply + autograd.grad of the input and all "
+                                                         "parameters: four convolutions, four input-gradient "
+                                                         "convolutions, four weight gradients"},
                "note": "CNN 5-32-32-32-5 (3x3x3, BF16 tensor cores: tcgen05 where the grid fits its tiles) "
                        "applied after every big step inside the step's CUDA graph (lexgb_set_sgs_net); CUDA "
                        "events over 300 (32^3) and 100 (128x128x64) steps each"}

@@ -1,30 +1,39 @@
 // kernels_cnn_tc.cu - the learned SGS correction's 3x3x3 convolution on the 5th-generation tensor
-// cores (tcgen05.mma, accumulators in tensor memory), as an implicit GEMM per tile of points:
+// cores (tcgen05.mma, accumulators in tensor memory), as an implicit GEMM per tile of points, one
+// input plane at a time:
 //
-//   D[128 points][N] = sum over the 27 offsets and the input channels of
-//                      A[128 points][Cin] (the input shifted by the offset) x B[Cin][N] (the offset's weights)
+//   D[128 points][3 NP] += A[128 points][Cin] (input plane p shifted by (dy, dx))
+//                          x B[Cin][3 NP]     (the weights of the taps (dz, dy, dx), dz = -1, 0, +1)
 //
-// A block owns a column of 8 (x) x 16 (y) points and marches up a chunk of levels, with its warps
-// specialised:
+// so that one MMA adds plane p's share to the three output levels it feeds (p+1, p, p-1): each
+// input tile is read by the tensor cores 9 x Cin/16 times per plane instead of 27 x Cin/16.
+// A block owns a column of 8 (x) x 16 (y) points and marches up a chunk of levels, with its
+// warps specialised:
 //   warp 4 (producer)  loads each input plane the chunk needs (10 x 18 points with the one-point
 //                      halo, zero outside the grid by the tensor map's out-of-bounds fill) by TMA
 //                      (cp.async.bulk.tensor, one box per 8-channel group) into a ring of plane
 //                      slots; a slot's full barrier completes on the bytes' arrival;
-//   warp 5 (MMA)       for level z waits for planes z-1, z, z+1 and for a free accumulator, issues
-//                      the 27 x Cin/16 MMAs (M = 128, N = Cout padded to a multiple of 16, K = 16,
-//                      BF16 in, FP32 accumulate) into one of two accumulators, and commits them
-//                      to the accumulator's full barrier and to plane z-1's empty barrier;
-//   warps 0-3          (the four tensor-memory lane quarters) wait for an accumulator, read their
-//                      32 rows (tcgen05.ld), free it, and apply the epilogue of k_conv3d_smem (bias,
-//                      FP32 pre-activation, GELU, padding channels zero, BF16 / FP32 output).
+//   warp 5 (MMA)       for plane p issues the 9 x Cin/16 MMAs (M = 128, N = 3 NP, K = 16, BF16
+//                      in, FP32 accumulate) into the columns of output levels p+1, p, p-1: the
+//                      tensor memory is a ring of Q level slots of NP columns in descending level
+//                      order, so the three are adjacent (where they wrap round the ring, the MMA
+//                      is split in two; never in a chunk of at most Q - 5 levels); it frees the
+//                      plane's slot and marks level p-1 summed;
+//   warps 0-3          (the four tensor-memory lane quarters) zero the ring first (the windows of
+//                      neighbouring planes overlap, so every MMA accumulates), then for each level
+//                      wait for it, read their 32 rows (tcgen05.ld), zero the level slot again if
+//                      a later level of the chunk uses it, hand it back to the MMA warp and apply
+//                      the epilogue of k_conv3d_smem (bias, FP32 pre-activation, GELU, padding
+//                      channels zero, BF16 / FP32 output).
 // Every wait is bounded: one that gives up counts a timeout in g_tc_timeouts and sets the block's
 // abort flag, which ends the other roles' waits; the block then waits (bounded) for the MMAs it
-// issued, frees its tensor memory and returns.
+// issued and the copies in flight, frees its tensor memory and returns.
 //
 // Shared-memory layouts (16-byte pieces; the tensor cores' canonical K-major layout without
 // swizzle, core matrix = 8 rows of 16 bytes):
-//   weights  Wsm[27][CIN/8][NP][8]         core matrix = 8 output channels x 8 inputs; K step
-//                                          NP x 16 B (LBO), next 8 output channels 128 B (SBO)
+//   weights  Wsm[9][CIN/8][3 NP][8]        (dy dx), input group, row t NP + co of tap (t - 1, dy,
+//                                          dx) and output channel co; core matrix = 8 rows x 8
+//                                          inputs; K step 3 NP x 16 B (LBO), next 8 rows 128 B (SBO)
 //   planes   Psm[R][CIN/8][18][10][8]      slot, channel group (its box padded to 128-byte
 //                                          alignment), row, x; core matrix = 8 consecutive x
 //                                          points; K step = the next channel group's box (LBO),
@@ -43,26 +52,33 @@ namespace {
 
 constexpr int TC_TX = 8, TC_TY = 16, TC_HX = TC_TX + 2, TC_HY = TC_TY + 2;
 constexpr int TC_THREADS = 192;               // 4 epilogue warps, the producer, the MMA warp
-constexpr int TC_TMEM_COLS = 128;             // allocated columns (2 accumulators of N <= 32)
 constexpr long long TC_POLLS = 1ll << 24;     // mbarrier polls before a wait gives up
 constexpr int TC_BOX_BYTES = TC_HY * TC_HX * 16;                  // one channel group's box: 2880
 constexpr int TC_GROUP_BYTES = (TC_BOX_BYTES + 127) / 128 * 128;  // padded to 128 bytes: 2944
 
 template <int CIN, int COUT>
 struct TcLayout {
-  static constexpr int NP = COUT < 16 ? 16 : COUT;  // N of the MMA (a multiple of 16 for M = 128)
+  static constexpr int NP = COUT < 16 ? 16 : COUT;  // output channels of one level in N (16 or 32)
+  static constexpr int N3 = 3 * NP;                 // N of the MMA: output levels p+1, p, p-1
   static constexpr int CG = CIN / 8;                // channel groups of 8 (16 bytes)
-  static constexpr int R = CIN == 32 ? 4 : 6;       // plane slots (two blocks per SM fit)
-  static constexpr int W_BYTES = 27 * CG * NP * 16;
+  static constexpr int R = 4;                       // plane slots (each plane is read once)
+  static constexpr int TMEM_COLS = 256;             // two blocks per SM
+  static constexpr int Q = TMEM_COLS / NP;          // level slots of NP columns (8 or 16)
+  static constexpr int W_BYTES = 9 * CG * N3 * 16;
   static constexpr int PLANE_BYTES = CG * TC_GROUP_BYTES;
   static constexpr int P_BYTES = R * PLANE_BYTES;
   static constexpr int A_LBO = TC_GROUP_BYTES;      // next channel group
   static constexpr int A_SBO = TC_HX * 16;          // next row of the tile (8 points on)
-  static constexpr int B_LBO = NP * 16;             // next input-channel group
-  static constexpr int B_SBO = 128;                 // next 8 output channels
-  static constexpr int BAR_BYTES = (2 * R + 4) * 8 + 16;
-  // + alignment slack, barriers, tensor-memory address, abort flag, bias
-  static constexpr size_t BYTES = 128 + (size_t)W_BYTES + P_BYTES + BAR_BYTES + NP * 4;
+  static constexpr int B_LBO = N3 * 16;             // next input-channel group
+  static constexpr int B_SBO = 128;                 // next 8 rows of N
+  static constexpr int EPI = 4;                     // epilogue warps (one per tensor-memory lane quarter)
+  static constexpr int THREADS = 32 * (EPI + 2);    // + the producer and the MMA warp
+  static constexpr int NBAR = 2 * R + 2 * Q + 1;    // full[R], empty[R], summed[Q], freed[Q], done
+  static constexpr int BAR_BYTES = NBAR * 8 + 16;
+  // + alignment slack, barriers, tensor-memory address, abort flag, bias; at least 80 KB, so that
+  // no more blocks share an SM than its tensor memory holds
+  static constexpr size_t NEED = 128 + (size_t)W_BYTES + P_BYTES + BAR_BYTES + NP * 4;
+  static constexpr size_t BYTES = NEED < 80 * 1024 ? 80 * 1024 : NEED;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -122,6 +138,24 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const v
   return false;
 }
 
+// Bounded wait with a back-off between polls (about a second at most), for the warps that wait out
+// the whole of a block's work; gives up early when the block's abort flag is set (if checked).
+__device__ __forceinline__ bool mbar_wait_long(uint32_t bar, uint32_t parity, const volatile int* abort) {
+  for (long long i = 0; i < (1ll << 22); ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (abort && *abort) return false;
+    __nanosleep(256);
+  }
+  return false;
+}
+
 // a 4-D box (channel, x, y, z) of a tensor map into shared memory, completing on an mbarrier
 __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c, int x, int y, int z,
                                             uint32_t bar) {
@@ -150,31 +184,70 @@ __device__ __forceinline__ void tmem_load16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+
+__device__ __forceinline__ void tmem_zero16(uint32_t taddr) {
+  const uint32_t z = 0;
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr),
+      "r"(z)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_zero8(uint32_t taddr) {
+  const uint32_t z = 0;
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1};" ::"r"(taddr), "r"(z)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_load8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+// CW consecutive columns of this warp's lanes: load / zero
+template <int CW>
+__device__ __forceinline__ void tmem_load_cols(uint32_t taddr, float* v) {
+#pragma unroll
+  for (int c = 0; c < CW; c += 16) {
+    if (CW - c >= 16) tmem_load16(taddr + (uint32_t)c, v + c);
+    else tmem_load8(taddr + (uint32_t)c, v + c);
+  }
+}
+template <int CW>
+__device__ __forceinline__ void tmem_zero_cols(uint32_t taddr) {
+#pragma unroll
+  for (int c = 0; c < CW; c += 16) {
+    if (CW - c >= 16) tmem_zero16(taddr + (uint32_t)c);
+    else tmem_zero8(taddr + (uint32_t)c);
+  }
+}
+
 template <int CIN, int COUT>
-__global__ void __launch_bounds__(TC_THREADS) k_conv3d_tc(const __grid_constant__ CUtensorMap xmap, int nx, int ny,
-                                                          int nz, int zc, const __nv_bfloat16* __restrict__ w,
-                                                          const float* __restrict__ bias, float* __restrict__ pre,
-                                                          __nv_bfloat16* __restrict__ ybf, float* __restrict__ yf,
-                                                          int gelu, int creal, int early_weights) {
+__global__ void __launch_bounds__(TcLayout<CIN, COUT>::THREADS, 1)
+    k_conv3d_tc(const __grid_constant__ CUtensorMap xmap, int nx, int ny, int nz, int zc,
+                const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias, float* __restrict__ pre,
+                __nv_bfloat16* __restrict__ ybf, float* __restrict__ yf, int gelu, int creal, int early_weights) {
   using L = TcLayout<CIN, COUT>;
-  constexpr int NP = L::NP, CG = L::CG, R = L::R;
+  constexpr int NP = L::NP, N3 = L::N3, CG = L::CG, R = L::R, Q = L::Q, EPI = L::EPI;
+  constexpr int H = EPI / 4, CW = NP / H;   // channel parts of a level; columns of one part
   extern __shared__ unsigned char tc_raw[];
   const uint32_t raw_s = smem_u32(tc_raw);
   unsigned char* smem = tc_raw + ((128u - (raw_s & 127u)) & 127u);   // 128-byte aligned for TMA
   const uint32_t w_s = smem_u32(smem), p_s = w_s + L::W_BYTES, bar_s = p_s + L::P_BYTES;
-  // barriers: full[R], empty[R], acc_full[2], acc_empty[2]; then the tensor-memory address and abort flag
   auto full = [&](int s) { return bar_s + 8u * s; };
   auto empty = [&](int s) { return bar_s + 8u * (R + s); };
-  auto acc_full = [&](int a) { return bar_s + 8u * (2 * R + a); };
-  auto acc_empty = [&](int a) { return bar_s + 8u * (2 * R + 2 + a); };
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + L::W_BYTES + L::P_BYTES + (2 * R + 4) * 8);
+  auto summed = [&](int q) { return bar_s + 8u * (2 * R + q); };       // a level slot's sums are complete
+  auto freed = [&](int q) { return bar_s + 8u * (2 * R + Q + q); };    // ... read (and zeroed if reused)
+  const uint32_t done = bar_s + 8u * (2 * R + 2 * Q);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + L::W_BYTES + L::P_BYTES + L::NBAR * 8);
   volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
   float* bsm = reinterpret_cast<float*>(smem + L::W_BYTES + L::P_BYTES + L::BAR_BYTES);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  if (warp == 5) {  // tensor memory for the two accumulators
+  if (warp == EPI + 1) {  // tensor memory: Q level slots of NP columns
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
-                 "r"(TC_TMEM_COLS)
+                 "r"(L::TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -183,39 +256,63 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3d_tc(const __grid_constant_
       mbar_init(full(s), 1);
       mbar_init(empty(s), 1);
     }
-    for (int a = 0; a < 2; ++a) {
-      mbar_init(acc_full(a), 1);
-      mbar_init(acc_empty(a), 4);
+    for (int q = 0; q < Q; ++q) {
+      mbar_init(summed(q), 1);
+      mbar_init(freed(q), EPI);
     }
+    mbar_init(done, 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // weights Wsm[tap][cg][n][8] from w[tap][COUT][CIN] (rows n >= COUT zero) and the bias, by cp.async
+  // weights Wsm[dy dx][cg][n][8] from w[tap][COUT][CIN]: row n = t NP + co holds the tap
+  // (dz = t - 1, dy, dx) of output channel co (rows co >= COUT zero), so that one MMA on input
+  // plane p adds to output levels p+1 (t = 0), p (t = 1) and p-1 (t = 2)
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   if (!early_weights) asm volatile("griddepcontrol.wait;" ::: "memory");
-  for (int e = tid; e < 27 * CG * NP; e += TC_THREADS) {
-    const int n = e % NP, cg = (e / NP) % CG, tap = e / (NP * CG);
-    const bool ok = n < COUT;
-    cp16(w_s + (uint32_t)e * 16u, w + ((long long)(tap * COUT + (ok ? n : 0)) * CIN + cg * 8), ok);
+  for (int e = tid; e < 9 * CG * N3; e += L::THREADS) {
+    const int n = e % N3, cg = (e / N3) % CG, yx = e / (N3 * CG);
+    const int t = n / NP, co = n % NP;
+    const bool ok = co < COUT;
+    const int tap = t * 9 + yx;
+    cp16(w_s + (uint32_t)e * 16u, w + ((long long)(tap * COUT + (ok ? co : 0)) * CIN + cg * 8), ok);
   }
   if (tid < NP) bsm[tid] = (bias && tid < COUT) ? bias[tid] : 0.f;
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+  // epilogue warp w: lanes 32 (w % 4) .., channels CW (w / 4) .. of every level
+  const uint32_t lanes = (uint32_t)(32 * (warp & 3)) << 16;
+  const int part = (warp >> 2) * CW;
+  // the MMA windows of neighbouring planes overlap, so they all accumulate: zero the slots first
+  if (warp < EPI) {
+    for (int q = 0; q < Q; ++q) tmem_zero_cols<CW>(tmem + lanes + (uint32_t)(q * NP + part));
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+  }
   asm volatile("cp.async.wait_all;" ::: "memory");
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // weights -> the tensor cores
   if (early_weights) asm volatile("griddepcontrol.wait;" ::: "memory");   // the input is ready
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tslot;
 
   const int tiles_x = nx / TC_TX, tiles_y = ny / TC_TY;
   const int tx = blockIdx.x % tiles_x, ty = (blockIdx.x / tiles_x) % tiles_y, ch = blockIdx.x / (tiles_x * tiles_y);
   const int x0 = tx * TC_TX, y0 = ty * TC_TY, z0 = ch * zc, z1 = min(z0 + zc, nz);
   const int p0 = z0 - 1;   // first plane of the chunk; plane p uses slot (p - p0) % R, fill (p - p0) / R
+  // Output level z (z0 - 2 .. z1 + 1; the four outside z0 .. z1 - 1 are scratch that the planes at
+  // the chunk's ends add to) lives in level slot Q - 1 - (z - z0 + 2) mod Q, its (z - z0 + 2) / Q-th
+  // use: the slots of levels p+1, p, p-1 follow one another except where they wrap round (never in
+  // a chunk of at most Q - 5 levels).
+  const int zb = z0 - 2;
+  auto lslot = [&](int z) { return Q - 1 - (z - zb) % Q; };
+  auto luse = [&](int z) { return (z - zb) / Q; };
 
-  if (warp == 4) {
+  if (warp == EPI) {
     // ---------------- producer: planes z0-1 .. z1 ----------------
     if (lane == 0) {
-      for (int p = p0; p <= z1; ++p) {
+      int p = p0;
+      for (; p <= z1; ++p) {
         const int s = (p - p0) % R, k = (p - p0) / R;
         if (k > 0 && !mbar_wait(empty(s), (k - 1) & 1, abort)) {
           atomicAdd(&g_tc_timeouts, 1u);
@@ -226,63 +323,62 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3d_tc(const __grid_constant_
         for (int cg = 0; cg < CG; ++cg)
           tma_load_4d(p_s + s * L::PLANE_BYTES + cg * TC_GROUP_BYTES, &xmap, cg * 8, x0 - 1, y0 - 1, p, full(s));
       }
+      // the copies this thread issued have landed before the block's memory goes (bounded)
+      for (int q = p - 1; q >= p0 && q >= p - R; --q) mbar_wait_long(full((q - p0) % R), ((q - p0) / R) & 1, nullptr);
     }
-  } else if (warp == 5) {
-    // ---------------- MMA issuer ----------------
+  } else if (warp == EPI + 1) {
+    // ---------------- MMA issuer: one plane at a time ----------------
     if (lane == 0) {
-      constexpr uint32_t idesc = tc_idesc(128, NP);
       // descriptors: the start address is the low field (16-byte units), so an operand at a fixed
       // offset from a base is the base's descriptor plus the offset / 16
       const uint64_t b0 = smem_desc(w_s, L::B_LBO, L::B_SBO);
       bool ok = true;
-      int issued = 0;
-      for (int z = z0; z < z1 && ok; ++z) {
-        const int i = z - z0, a = i & 1;
-        // planes z-1, z (already complete after the first level) and z+1
-        for (int p = (z == z0 ? z - 1 : z + 1); p <= z + 1 && ok; ++p) {
-          const int s = (p - p0) % R, k = (p - p0) / R;
-          ok = mbar_wait(full(s), k & 1, abort);
-        }
-        if (ok && i >= 2) ok = mbar_wait(acc_empty(a), ((i >> 1) - 1) & 1, abort);
+      for (int p = p0; p <= z1 && ok; ++p) {
+        const int s = (p - p0) % R, k = (p - p0) / R;
+        ok = mbar_wait(full(s), k & 1, abort);
+        // level p+1 is new in its slot: the level that used the slot before has been read and zeroed
+        if (ok && luse(p + 1) > 0) ok = mbar_wait(freed(lslot(p + 1)), (luse(p + 1) - 1) & 1, abort);
         if (!ok) {
           atomicAdd(&g_tc_timeouts, 1u);
           *abort = 1;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        uint32_t acc = 0;
+        const int q0 = lslot(p + 1);   // slots q0, q0 + 1, q0 + 2 (mod Q) <- t = 0, 1, 2
+        // the rows t < split go to columns q0 NP.., the rest to column 0 (the window wraps)
+        const int split = q0 + 3 <= Q ? 3 : Q - q0;
+        const uint32_t c_hi = tmem + (uint32_t)(q0 * NP), c_lo = tmem;
+        const uint64_t a0 = smem_desc(p_s + s * L::PLANE_BYTES, L::A_LBO, L::A_SBO);
 #pragma unroll
-        for (int dz = 0; dz < 3; ++dz) {
-          const uint32_t plane = p_s + ((z - 1 + dz - p0) % R) * L::PLANE_BYTES;
-          const uint64_t a0 = smem_desc(plane, L::A_LBO, L::A_SBO);
+        for (int dy = 0; dy < 3; ++dy)
 #pragma unroll
-          for (int dy = 0; dy < 3; ++dy)
+          for (int dx = 0; dx < 3; ++dx)
 #pragma unroll
-            for (int dx = 0; dx < 3; ++dx)
-#pragma unroll
-              for (int ks = 0; ks < CIN / 16; ++ks) {
-                const int tap = dz * 9 + dy * 3 + dx;
-                const uint64_t ad = a0 + (uint64_t)((2 * ks * TC_GROUP_BYTES + (dy * TC_HX + dx) * 16) >> 4);
-                const uint64_t bd = b0 + (uint64_t)(((tap * CG + 2 * ks) * NP * 16) >> 4);
-                mma_bf16_tc(tmem + (uint32_t)(a * NP), ad, bd, idesc, acc);
-                acc = 1;
+            for (int ks = 0; ks < CIN / 16; ++ks) {
+              const uint64_t ad = a0 + (uint64_t)((2 * ks * TC_GROUP_BYTES + (dy * TC_HX + dx) * 16) >> 4);
+              const uint64_t bd = b0 + (uint64_t)((((dy * 3 + dx) * CG + 2 * ks) * N3 * 16) >> 4);
+              if (split == 3) {
+                mma_bf16_tc(c_hi, ad, bd, tc_idesc(128, N3), 1u);
+              } else if (split == 2) {
+                mma_bf16_tc(c_hi, ad, bd, tc_idesc(128, 2 * NP), 1u);
+                mma_bf16_tc(c_lo, ad, bd + (uint64_t)((2 * NP * 16) >> 4), tc_idesc(128, NP), 1u);
+              } else {
+                mma_bf16_tc(c_hi, ad, bd, tc_idesc(128, NP), 1u);
+                mma_bf16_tc(c_lo, ad, bd + (uint64_t)((NP * 16) >> 4), tc_idesc(128, 2 * NP), 1u);
               }
-        }
-        mma_commit(acc_full(a));
-        mma_commit(empty((z - 1 - p0) % R));   // plane z-1 is not read again
-        ++issued;
+            }
+        mma_commit(empty(s));               // plane p is not read again
+        mma_commit(summed(lslot(p - 1)));   // level p-1 has all three of its planes
       }
-      if (!ok && issued > 0) {  // the last commit before the abort: a bounded wait before the memory goes
-        const int i = issued - 1;
-        mbar_wait(acc_full(i & 1), (i >> 1) & 1, abort);
-      }
+      mma_commit(done);
+      mbar_wait_long(done, 0, nullptr);   // the MMAs are complete before the tensor memory goes
     }
   } else {
-    // ---------------- epilogue: warps 0-3, tensor-memory lanes 32 warp .. 32 warp + 31 ----------------
-    const int r = 32 * warp + lane;   // row r <-> point (x0 + r % 8, y0 + r / 8)
-    for (int z = z0; z < z1; ++z) {
-      const int i = z - z0, a = i & 1;
-      if (!__all_sync(0xffffffffu, mbar_wait(acc_full(a), (i >> 1) & 1, abort))) {   // warp-uniform
+    // ---------------- epilogue: warps 0 .. EPI-1 ----------------
+    const int r = 32 * (warp & 3) + lane;   // row r <-> point (x0 + r % 8, y0 + r / 8)
+    for (int z = zb; z < z1; ++z) {
+      const int q = lslot(z);
+      if (!__all_sync(0xffffffffu, mbar_wait(summed(q), luse(z) & 1, abort))) {   // warp-uniform
         if (lane == 0) {
           atomicAdd(&g_tc_timeouts, 1u);
           *abort = 1;
@@ -290,54 +386,63 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3d_tc(const __grid_constant_
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      float v[NP];
-#pragma unroll
-      for (int c = 0; c < NP; c += 16) tmem_load16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(a * NP + c), v + c);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      float v[CW];
+      const bool real = z >= z0;
+      const uint32_t cols = tmem + lanes + (uint32_t)(q * NP + part);
+      if (real) {
+        tmem_load_cols<CW>(cols, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      }
+      if (z + Q <= z1 + 1) {   // the slot's next level is in this chunk: zero it for that level
+        tmem_zero_cols<CW>(cols);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(acc_empty(a));   // the accumulator may be overwritten
-      // the point's COUT channels as 16-byte stores (COUT x 2 bytes BF16, COUT x 4 bytes FP32)
+      if (lane == 0) mbar_arrive(freed(q));
+      if (!real || part >= COUT) continue;
+      // the point's channels part .. part + CW - 1 (those below COUT) as 16-byte stores
       const long long p = ((long long)z * ny + y0 + r / TC_TX) * nx + x0 + r % TC_TX;
+      constexpr int CN = CW < COUT ? CW : COUT;   // channels of this part below COUT (COUT % CW == 0 or COUT < CW)
 #pragma unroll
-      for (int co = 0; co < COUT; ++co) v[co] += bsm[co];
+      for (int c = 0; c < CN; ++c) v[c] += bsm[part + c];
       if (pre) {
 #pragma unroll
-        for (int co = 0; co < COUT; co += 4)
-          *reinterpret_cast<float4*>(pre + p * COUT + co) = make_float4(v[co], v[co + 1], v[co + 2], v[co + 3]);
+        for (int c = 0; c < CN; c += 4)
+          *reinterpret_cast<float4*>(pre + p * COUT + part + c) = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
       }
 #pragma unroll
-      for (int co = 0; co < COUT; ++co) {
-        const float t = gelu ? gelu_fast(v[co]) : v[co];
-        v[co] = co < creal ? t : 0.f;
+      for (int c = 0; c < CN; ++c) {
+        const float t = gelu ? gelu_fast(v[c]) : v[c];
+        v[c] = part + c < creal ? t : 0.f;
       }
       if (ybf) {
 #pragma unroll
-        for (int co = 0; co < COUT; co += 8) {
-          uint4 q;
-          __nv_bfloat162 h0 = __floats2bfloat162_rn(v[co], v[co + 1]);
-          __nv_bfloat162 h1 = __floats2bfloat162_rn(v[co + 2], v[co + 3]);
-          __nv_bfloat162 h2 = __floats2bfloat162_rn(v[co + 4], v[co + 5]);
-          __nv_bfloat162 h3 = __floats2bfloat162_rn(v[co + 6], v[co + 7]);
-          q.x = *reinterpret_cast<uint32_t*>(&h0);
-          q.y = *reinterpret_cast<uint32_t*>(&h1);
-          q.z = *reinterpret_cast<uint32_t*>(&h2);
-          q.w = *reinterpret_cast<uint32_t*>(&h3);
-          *reinterpret_cast<uint4*>(ybf + p * COUT + co) = q;
+        for (int c = 0; c < CN; c += 8) {
+          uint4 qq;
+          __nv_bfloat162 h0 = __floats2bfloat162_rn(v[c], v[c + 1]);
+          __nv_bfloat162 h1 = __floats2bfloat162_rn(v[c + 2], v[c + 3]);
+          __nv_bfloat162 h2 = __floats2bfloat162_rn(v[c + 4], v[c + 5]);
+          __nv_bfloat162 h3 = __floats2bfloat162_rn(v[c + 6], v[c + 7]);
+          qq.x = *reinterpret_cast<uint32_t*>(&h0);
+          qq.y = *reinterpret_cast<uint32_t*>(&h1);
+          qq.z = *reinterpret_cast<uint32_t*>(&h2);
+          qq.w = *reinterpret_cast<uint32_t*>(&h3);
+          *reinterpret_cast<uint4*>(ybf + p * COUT + part + c) = qq;
         }
       }
       if (yf) {
 #pragma unroll
-        for (int co = 0; co < COUT; co += 4)
-          *reinterpret_cast<float4*>(yf + p * COUT + co) = make_float4(v[co], v[co + 1], v[co + 2], v[co + 3]);
+        for (int c = 0; c < CN; c += 4)
+          *reinterpret_cast<float4*>(yf + p * COUT + part + c) = make_float4(v[c], v[c + 1], v[c + 2], v[c + 3]);
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 5) {
+  if (warp == EPI + 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L::TMEM_COLS) : "memory");
   }
 }
 
@@ -393,24 +498,6 @@ __device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map
       "%5, %6}], [%7];" ::"r"(dst),
       "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
       : "memory");
-}
-
-// Bounded wait with a back-off between polls (about a second at most), for the warps that wait out
-// the whole of a block's work; gives up early when the block's abort flag is set (if checked).
-__device__ __forceinline__ bool mbar_wait_long(uint32_t bar, uint32_t parity, const volatile int* abort) {
-  for (long long i = 0; i < (1ll << 22); ++i) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (abort && *abort) return false;
-    __nanosleep(256);
-  }
-  return false;
 }
 
 template <int CG, int NP>
@@ -571,7 +658,7 @@ cudaError_t tc_grid(int* cap) {
     if (e != cudaSuccess) return e;
     int sms = 0, per = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv3d_tc<CIN, COUT>, TC_THREADS, L::BYTES)) !=
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv3d_tc<CIN, COUT>, L::THREADS, L::BYTES)) !=
         cudaSuccess)
       return e;
     grid_cap[dev] = sms * (per < 1 ? 1 : per);
@@ -625,21 +712,24 @@ cudaError_t launch_tc(int nx, int ny, int nz, const void* x, const __nv_bfloat16
   if (!make_xmap(&xmap, x, nx, ny, nz, CIN)) return cudaErrorInvalidValue;
   // level chunks of at least 4 levels: the count whose blocks fill their waves of resident blocks
   // best (ties: fewer chunks, since every chunk stages the weights and two extra planes)
+  using L = TcLayout<CIN, COUT>;
   const int tiles = (nx / TC_TX) * (ny / TC_TY);
   int zc = nz;
   double best = -1.0;
   for (int nch = 1; nch <= (nz + 3) / 4; ++nch) {
-    const int z = (nz + nch - 1) / nch, blocks = tiles * ((nz + z - 1) / z);
+    const int z = (nz + nch - 1) / nch;
+    const long long blocks = (long long)tiles * ((nz + z - 1) / z);
     const double fill = (double)blocks / ((double)((blocks + cap - 1) / cap) * cap);
     if (fill > best + 1e-9) {
       best = fill;
       zc = z;
     }
   }
+  if ((long long)tiles * ((nz + zc - 1) / zc) > 0x7fffffffll) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(tiles * ((nz + zc - 1) / zc)));
-  cfg.blockDim = dim3(TC_THREADS);
-  cfg.dynamicSmemBytes = TcLayout<CIN, COUT>::BYTES;
+  cfg.blockDim = dim3(L::THREADS);
+  cfg.dynamicSmemBytes = L::BYTES;
   cfg.stream = st;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
