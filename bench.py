@@ -487,6 +487,63 @@ def profile_sgs(args):
     print(json.dumps({"profile_sgs": True, "steps": args.steps, "warmup": args.warmup}))
 
 
+def profile_cnn(args):
+    """CUDA-event times of the correction's layer shapes at --sgs-dims (default here 128,128,64):
+    lexgb_cnn_conv3d without the FP32 pre-activation (as in the step graph) and
+    lexgb_cnn_conv3d_dw, each on the tcgen05 kernel and on the legacy one (mma.sync convolution,
+    FP32 CUDA-core weight gradient); --steps launches each after --warmup."""
+    import ctypes
+    import torch
+    from lex_gb300 import _lib
+    lib = _lib.load()
+    dims = tuple(int(v) for v in args.sgs_dims.split(","))
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    gen = torch.Generator(device="cpu").manual_seed(7)
+    P = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+    def timed(call, reps):
+        for _ in range(args.warmup):
+            _lib.check(call())
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps * 1e3
+
+    out = {"profile_cnn": True, "grid": list(dims), "unit": "us per launch", "layers": {}}
+    for cin, cout, gstride in ((16, 32, 32), (32, 32, 32), (32, 8, 16)):
+        x = torch.randn(n, cin, generator=gen).to(torch.bfloat16).cuda()
+        w = (0.2 * torch.randn(27, cout, cin, generator=gen)).to(torch.bfloat16).cuda()
+        b = torch.randn(cout, generator=gen).cuda()
+        g = torch.randn(n, gstride, generator=gen).to(torch.bfloat16).cuda()
+        yb = torch.empty(n, cout, dtype=torch.bfloat16, device="cuda")
+        yf = torch.empty(n, cout, device="cuda")
+        dw = torch.zeros(27, cout, cin, device="cuda")
+        last = cout == 8
+        flop = 2 * 27 * cin * cout * n
+        rec = {}
+        for name, code in (("tcgen05", 2), ("legacy", 1)):
+            _lib.check(lib.lexgb_cnn_set_kernel(code))
+            conv = lambda: lib.lexgb_cnn_conv3d(nx, ny, nz, cin, cout, P(x), P(w), P(b), None,
+                                                None if last else P(yb), P(yf) if last else None,
+                                                0 if last else 1, 5 if last else cout, None)
+            dwc = lambda: lib.lexgb_cnn_conv3d_dw(nx, ny, nz, cin, cout, gstride, P(x), P(g), P(dw), None, None)
+            tc = timed(conv, args.steps)
+            td = timed(dwc, args.steps if name == "tcgen05" else max(1, args.steps // 10))
+            rec[name] = {"conv3d": tc, "conv3d_dw": td, "conv3d_tflops": flop / tc / 1e6,
+                         "conv3d_dw_tflops": flop / td / 1e6}
+        _lib.check(lib.lexgb_cnn_set_kernel(0))
+        out["layers"]["%d->%d" % (cin, cout)] = rec
+    t = ctypes.c_uint(0)
+    _lib.check(lib.lexgb_cnn_take_timeouts(ctypes.byref(t)))
+    out["tcgen05_timeouts"] = t.value
+    print(json.dumps(out))
+
+
 def profile_adjoint(args):
     """Warm-up + timed forward-with-intermediates + reverse passes of the benchmarked step
     (lexgb_step_keep + lexgb_step_vjp_kept), for profiler captures."""
@@ -526,7 +583,11 @@ def main():
     ap.add_argument("--profile", action="store_true", help="only warm-up + timed steps (profiler captures)")
     ap.add_argument("--profile-sgs", action="store_true",
                     help="only a few coarse 32^3 steps with the fused learned SGS correction (profiler captures)")
-    ap.add_argument("--sgs-dims", default="32,32,32", help="nx,ny,nz of --profile-sgs")
+    ap.add_argument("--profile-cnn", action="store_true",
+                    help="only CUDA-event times of the correction's convolutions and weight gradients, tcgen05 "
+                         "against the legacy kernels, at --sgs-dims")
+    ap.add_argument("--sgs-dims", default=None, help="nx,ny,nz of --profile-sgs (32,32,32) / --profile-cnn "
+                                                      "(128,128,64)")
     ap.add_argument("--acoustic-kernel", default="auto", choices=["auto", "rows", "tile", "persistent"],
                     help="form of the acoustic sub-steps (auto: the fastest measured for the grid)")
     ap.add_argument("--profile-adjoint", action="store_true",
@@ -534,8 +595,12 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "lexgb":
         args.warmup = 3
+    if args.sgs_dims is None:
+        args.sgs_dims = "128,128,64" if args.profile_cnn else "32,32,32"
     if args.profile_sgs:
         profile_sgs(args)
+    elif args.profile_cnn:
+        profile_cnn(args)
     elif args.profile_adjoint:
         profile_adjoint(args)
     elif args.impl == "reference":
