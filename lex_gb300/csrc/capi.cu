@@ -1292,12 +1292,10 @@ int adj_reverse(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages, const fl
       CK(launch_acoustic_vjp(d, c->ph, c->cols, a, (float)p.dtau[s], c->stream, awin_on ? &awin : nullptr));
       for (int f = 0; f < 4; ++f) adj[f] = o[f];
     }
-    CK(launch_axpy(w.Xb0.u, adj[0], faces, c->stream));
-    CK(launch_axpy(w.Xb0.v, adj[1], faces, c->stream));
-    CK(launch_axpy(w.Xb0.w, adj[2], faces, c->stream));
-    CK(launch_axpy(w.Xb0.p, adj[3], faces, c->stream));
-    // slow tendencies, theta/qv update, theta_rho, pi'_s
+    // slow tendencies, theta/qv update, theta_rho, pi'_s; the acoustic loop's input adjoints go to
+    // the big step's input adjoint in the same pass
     StageVjpArgs sa{};
+    for (int f = 0; f < 4; ++f) sa.acb[f] = adj[f];
     sa.xs = xs;
     sa.div = w.div[s];
     sa.Tnb = w.Cur.T;

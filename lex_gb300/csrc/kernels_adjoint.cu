@@ -446,9 +446,13 @@ __global__ void __launch_bounds__(AB) k_stage_pointwise_vjp(Dims d, Phys ph, Col
     }
     a.cb[2][id] = cw;
     a.xsb.w[id] += wb;
+    a.x0b.w[id] += LD(a.acb[2], id);   // the acoustic loop starts from the big step's input winds and pi'
     if (a.sgsb_w && k >= 1 && k < nz) a.sgsb_w[id] += Rw;
   }
   if (k >= nz) return;
+  a.x0b.u[id] += LD(a.acb[0], id);
+  a.x0b.v[id] += LD(a.acb[1], id);
+  a.x0b.p[id] += LD(a.acb[3], id);
   const float ri = c.rho_inv[k];   // products with the correctly rounded 1 / rho0 instead of divisions
   // ---- scalars
   const float Tb = LD(a.Tnb, id), Qb = LD(a.qnb, id);

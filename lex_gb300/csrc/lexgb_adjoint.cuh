@@ -23,6 +23,7 @@ struct StageVjpArgs {
   float dts;
   State xsb;                                  // adjoint of the stage input (accumulated)
   State x0b;                                  // adjoint of the big step's input (T, q accumulated)
+  const float* acb[4];                        // adjoint of the acoustic loop's input u, v, w, pi' (added to x0b)
   float* cb[5];                               // adjoint of the flux convergence per field (u, v, w, T, q)
   float* divb;                                // adjoint of the mass divergence (written)
   float *sgsb_u, *sgsb_v, *sgsb_w, *sgsb_T, *sgsb_q;  // SGS tendency adjoints (accumulated; null: off)
