@@ -2,7 +2,7 @@
 
 Tolerances are relative L2 norms of FP32 GPU results against FP64 references:
   * single operators on a random state ........................ 2e-6 (WENO operators 5e-6)
-  * RK stage tendencies (the reference's tends tuple) ........... 1e-5 (the spec bar)
+  * RK stage tendencies (the reference's tends tuple) ........... 1e-5
   * prognostic states: the error must stay within 1e-5 of the increment (state - initial
     state) plus the FP32 representation floor of the stored field, STATE_FLOOR * ||field||
     (theta is stored as theta - theta_ref, so its floor is taken on theta - theta_ref).
