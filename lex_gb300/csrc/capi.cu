@@ -1320,12 +1320,9 @@ int adj_reverse(lexgb_ctx* c, AdjWork& w, const State& x0, int nstages, const fl
     for (int f = 0; f < 4; ++f) aa.mb[f] = w.mb[f];
     aa.xsb = w.Xs;
     CK(launch_adv_vjp(d, c->ph, c->cols, aa, c->stream));
-    CK(launch_massdiv_vjp(d, c->ph, c->cols, w.divb, w.Xs, c->stream));
-    if (s == 0) {
-      for (int f = 0; f < NFIELD; ++f) CK(launch_axpy(field_of(w.Xb0, f), field_of(w.Xs, f), faces, c->stream));
-    } else {
-      std::swap(w.Cur, w.Xs);
-    }
+    // the first stage's input is the big step's input: its adjoint goes to Xb0 in the same pass
+    CK(launch_massdiv_vjp(d, c->ph, c->cols, w.divb, w.Xs, c->stream, s == 0 ? w.Xb0 : State{}));
+    if (s > 0) std::swap(w.Cur, w.Xs);
   }
   // the SGS tendencies were taken from the step's input state
   if (turb) {

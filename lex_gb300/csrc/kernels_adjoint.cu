@@ -519,18 +519,28 @@ __global__ void __launch_bounds__(AB) k_stage_pointwise_vjp(Dims d, Phys ph, Col
 }
 
 // mass divergence: xsb winds += div^T(divb)
-__global__ void __launch_bounds__(AB) k_massdiv_vjp(Dims d, Phys ph, Cols c, const float* __restrict__ divb, State xsb) {
+// and, with x0b (the first stage, whose input is the big step's input): x0b += xsb, all six fields
+__global__ void __launch_bounds__(AB) k_massdiv_vjp(Dims d, Phys ph, Cols c, const float* __restrict__ divb, State xsb,
+                                                    State x0b) {
   const long long t = (long long)blockIdx.x * AB + threadIdx.x;
   const int nx = d.nx, ny = d.ny, nz = d.nz, plane = d.plane();
   if (t >= d.faces()) return;
   const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / plane);
   const int id = (int)t;
   if (k >= 1 && k < nz) xsb.w[id] += c.rho_face0[k] * (LD(divb, id - plane) - LD(divb, id)) * ph.rdz;
+  if (x0b.w) x0b.w[id] += xsb.w[id];
   if (k >= nz) return;
   const float r = c.rho[k];
   const int row = k * plane;
   xsb.u[id] += r * (LD(divb, row + j * nx + wrapx(i - 1, nx)) - LD(divb, id)) * ph.rdx;
   xsb.v[id] += r * (LD(divb, row + wrapx(j - 1, ny) * nx + i) - LD(divb, id)) * ph.rdy;
+  if (x0b.u) {
+    x0b.u[id] += xsb.u[id];
+    x0b.v[id] += xsb.v[id];
+    x0b.T[id] += xsb.T[id];
+    x0b.q[id] += xsb.q[id];
+    x0b.p[id] += xsb.p[id];
+  }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -965,9 +975,9 @@ cudaError_t launch_stage_pointwise_vjp(const Dims& d, const Phys& ph, const Cols
 }
 
 cudaError_t launch_massdiv_vjp(const Dims& d, const Phys& ph, const Cols& c, const float* divb, State xsb,
-                               cudaStream_t st) {
+                               cudaStream_t st, State x0b) {
   const unsigned g = (unsigned)((d.faces() + AB - 1) / AB);
-  k_massdiv_vjp<<<g, AB, 0, st>>>(d, ph, c, divb, xsb);
+  k_massdiv_vjp<<<g, AB, 0, st>>>(d, ph, c, divb, xsb, x0b);
   return cudaGetLastError();
 }
 

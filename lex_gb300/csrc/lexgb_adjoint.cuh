@@ -63,7 +63,9 @@ cudaError_t launch_smag_vjp(const Dims&, const Phys&, const Cols&, State x0, con
 cudaError_t launch_acoustic_vjp(const Dims&, const Phys&, const Cols&, const AcousticVjpArgs&, float dtau,
                                 cudaStream_t, const cudaAccessPolicyWindow* win = nullptr);
 cudaError_t launch_stage_pointwise_vjp(const Dims&, const Phys&, const Cols&, const StageVjpArgs&, cudaStream_t);
-cudaError_t launch_massdiv_vjp(const Dims&, const Phys&, const Cols&, const float* divb, State xsb, cudaStream_t);
+// x0b (non-null fields): also x0b += xsb, after the update (the first stage's input is the step's input)
+cudaError_t launch_massdiv_vjp(const Dims&, const Phys&, const Cols&, const float* divb, State xsb, cudaStream_t,
+                               State x0b = State{});
 cudaError_t launch_adv_vjp(const Dims&, const Phys&, const Cols&, const AdvVjpArgs&, cudaStream_t);
 // y += x over n floats
 cudaError_t launch_axpy(float* y, const float* x, size_t n, cudaStream_t);
